@@ -1,0 +1,132 @@
+/*
+ * leopard_gb300.h -- C ABI of the GB300 (sm_103a) 2DTM search library.
+ *
+ * Plain pointers and sizes only; every pointer argument marked "device" must
+ * point to memory on the current CUDA device, and `stream` is a cudaStream_t
+ * (NULL = legacy default stream).  All calls are asynchronous on `stream`
+ * unless stated otherwise and return an lgb_status (0 = success).
+ *
+ * Reference interfaces these entry points replace (Leopard-EM, paths inside
+ * the Leopard-EM source tree):
+ *   lgb_match_init_stats      core_match_template.py:472-486
+ *                             (mip=-inf, best index=-1, sums=0 in
+ *                             _core_match_template_single_gpu)
+ *   lgb_match_prepare_image   core_match_template.py:446 (image_dft.to(device))
+ *   lgb_match_filters         core_match_template.py:274
+ *                             (projective_filters = ctf * whitening)
+ *   lgb_match_search          core_match_template.py:492-550, the orientation
+ *                             loop: roma.euler_to_rotmat (:506-508), the
+ *                             cross-correlation of cross_correlation.py:13-154
+ *                             and do_iteration_statistics_updates
+ *                             (backend/utils.py:191-255), fused
+ *   lgb_match_finalize        core_match_template.py:337-349 ->
+ *                             process_results.py:67-183
+ *                             (decode_global_search_index, scale_mip)
+ */
+#ifndef LEOPARD_GB300_H
+#define LEOPARD_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum lgb_status {
+  LGB_OK = 0,
+  LGB_ERR_INVALID_ARGUMENT = 1, /* null pointer, negative count, bad range   */
+  LGB_ERR_UNSUPPORTED_SIZE = 2, /* an FFT length outside the compiled set    */
+  LGB_ERR_WORKSPACE_TOO_SMALL = 3,
+  LGB_ERR_CUDA = 4,             /* a CUDA runtime call or launch failed      */
+  LGB_ERR_DEVICE_TIMEOUT = 5    /* a bounded device-side wait ran out        */
+} lgb_status;
+
+/* Shape of one whole-orientation search (one micrograph). */
+typedef struct lgb_match_problem {
+  int image_h;            /* H: real-space micrograph rows                         */
+  int image_w;            /* W: real-space micrograph columns (even)               */
+  int template_size;      /* d: cubic template edge; projections are d x d        */
+  int n_pixel_sizes;      /* C: leading axis of the projective-filter stack       */
+  int n_defocus;          /* D: second axis of the projective-filter stack        */
+  int n_orientations;     /* N: rows of the Euler-angle table                     */
+  int orientation_batch;  /* B: orientations correlated per statistics update     */
+} lgb_match_problem;
+
+/* Kernel stages of one orientation batch inside lgb_match_search. */
+enum {
+  LGB_STAGE_SLICE = 0,    /* Fourier slice extraction                          */
+  LGB_STAGE_PROJ_COL = 1, /* projective filter + inverse FFT along y           */
+  LGB_STAGE_PROJ_ROW = 2, /* c2r along x, ifftshift, projection moments        */
+  LGB_STAGE_PAD_RFFT = 3, /* normalisation + zero-padded row rfft              */
+  LGB_STAGE_COLPASS = 4,  /* column FFT, cross power, inverse column FFT       */
+  LGB_STAGE_ROWPASS = 5,  /* row c2r + MIP / index / sum statistics            */
+  LGB_N_STAGES = 6
+};
+
+/* Human-readable text of a status code (static storage). */
+const char* lgb_status_string(int status);
+
+/* Library version, major*10000 + minor*100 + patch. */
+int lgb_version(void);
+
+/* Stage profiler (no reference counterpart; measurement only).  Between
+ * lgb_profile_begin and lgb_profile_end every stage launch made by
+ * lgb_match_search on any stream is bracketed by CUDA events on that stream.
+ * lgb_profile_end waits for the recorded events and writes, per stage, the
+ * summed device milliseconds and the launch count (arrays of n_stages >=
+ * LGB_N_STAGES entries). */
+int lgb_profile_begin(void);
+int lgb_profile_end(double* stage_ms, long long* stage_launches, int n_stages);
+
+/* 1 if every FFT length this problem needs is compiled in, else 0. */
+int lgb_match_supported(const lgb_match_problem* problem);
+
+/* Bytes of device scratch that lgb_match_search needs for `problem`. */
+int lgb_match_workspace_size(const lgb_match_problem* problem, size_t* bytes);
+
+/* mip <- -inf, best_index <- -1, corr_sum <- 0, corr_sq_sum <- 0 over n_pixels. */
+int lgb_match_init_stats(long long n_pixels, float* mip, int* best_index, double* corr_sum,
+                         double* corr_sq_sum, void* stream);
+
+/* Copy the image spectrum (device, complex64 [H][W/2+1], row-major) into the
+ * workspace's padded layout.  Must precede lgb_match_search on a workspace. */
+int lgb_match_prepare_image(const lgb_match_problem* problem, const void* image_dft, void* workspace,
+                            size_t workspace_bytes, void* stream);
+
+/* projective_filters[c][d][y][x] = ctf_filters[c][d][y][x] * whitening[y][x]
+ * over C x D x d x (d/2+1) floats (device pointers). */
+int lgb_match_filters(const lgb_match_problem* problem, const float* ctf_filters, const float* whitening,
+                      float* projective_filters, void* stream);
+
+/* Correlate orientations [orientation_begin, orientation_end) in batches of
+ * problem->orientation_batch against the prepared image and fold every
+ * correlogram into the four per-pixel statistics maps (device, H x W):
+ *   mip          running maximum (strict '>' across batches, first index wins)
+ *   best_index   global search index  cs*D*N + df*N + orientation  (int32)
+ *   corr_sum     running sum (FP64)
+ *   corr_sq_sum  running sum of squares (FP64)
+ * template_dft: device complex64 [d][d][d/2+1], fftshifted over the first two
+ *   axes (volume_to_rfft_fourier_slice layout).
+ * projective_filters: device float [C][D][d][d/2+1].
+ * euler_angles: device float [N][3], ZYZ (phi, theta, psi) in degrees. */
+int lgb_match_search(const lgb_match_problem* problem, const void* template_dft, const float* projective_filters,
+                     const float* euler_angles, int orientation_begin, int orientation_end, float* mip,
+                     int* best_index, double* corr_sum, double* corr_sq_sum, void* workspace,
+                     size_t workspace_bytes, void* stream);
+
+/* Decode the best index and turn the sums into mean, standard deviation and
+ * z-score (FP64 arithmetic, FP32 outputs; all maps device, H x W):
+ *   corr_mean = S/total, corr_std = sqrt(max(S2/total - mean^2, 0)),
+ *   scaled_mip = (mip - mean)/std, or 0 where std == 0.
+ * `total_positions` is N*D*C of the whole search. */
+int lgb_match_finalize(const lgb_match_problem* problem, long long total_positions, const float* mip,
+                       const int* best_index, const double* corr_sum, const double* corr_sq_sum,
+                       const float* euler_angles, const float* defocus_values, float* scaled_mip,
+                       float* best_phi, float* best_theta, float* best_psi, float* best_defocus,
+                       float* corr_mean, float* corr_std, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LEOPARD_GB300_H */

@@ -1,0 +1,116 @@
+"""ctypes binding of the C ABI in ``include/leopard_gb300.h``.
+
+The library is the in-tree ``_build/libleopard_gb300.so`` produced by
+``leopard_em_gb300.build``.  There is no fallback: if the library is missing
+or a call fails, a RuntimeError (ValueError for bad arguments) is raised.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+_LOCK = threading.Lock()
+_LIB = None
+
+LGB_OK = 0
+LGB_ERR_INVALID_ARGUMENT = 1
+LGB_ERR_UNSUPPORTED_SIZE = 2
+LGB_ERR_WORKSPACE_TOO_SMALL = 3
+LGB_ERR_CUDA = 4
+LGB_ERR_DEVICE_TIMEOUT = 5
+
+
+class MatchProblem(ctypes.Structure):
+    """Mirror of ``lgb_match_problem``."""
+
+    _fields_ = [
+        ("image_h", ctypes.c_int),
+        ("image_w", ctypes.c_int),
+        ("template_size", ctypes.c_int),
+        ("n_pixel_sizes", ctypes.c_int),
+        ("n_defocus", ctypes.c_int),
+        ("n_orientations", ctypes.c_int),
+        ("orientation_batch", ctypes.c_int),
+    ]
+
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_LL = ctypes.c_longlong
+_SZ = ctypes.c_size_t
+_PROB = ctypes.POINTER(MatchProblem)
+
+_SIGNATURES = {
+    "lgb_status_string": ([_I], ctypes.c_char_p),
+    "lgb_version": ([], _I),
+    "lgb_profile_begin": ([], _I),
+    "lgb_profile_end": ([ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_LL), _I], _I),
+    "lgb_match_supported": ([_PROB], _I),
+    "lgb_match_workspace_size": ([_PROB, ctypes.POINTER(_SZ)], _I),
+    "lgb_match_init_stats": ([_LL, _P, _P, _P, _P, _P], _I),
+    "lgb_match_prepare_image": ([_PROB, _P, _P, _SZ, _P], _I),
+    "lgb_match_filters": ([_PROB, _P, _P, _P, _P], _I),
+    "lgb_match_search": ([_PROB, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _SZ, _P], _I),
+    "lgb_match_finalize": ([_PROB, _LL, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
+}
+
+
+STAGE_NAMES = ("slice", "proj_col", "proj_row", "pad_rfft", "colpass", "rowpass")
+
+
+class StageProfile:
+    """Context manager: per-stage device time (ms) and launch counts of every
+    lgb_match_search call made inside the ``with`` block."""
+
+    def __enter__(self):
+        check(lib().lgb_profile_begin(), "lgb_profile_begin")
+        self.ms = {}
+        self.launches = {}
+        return self
+
+    def __exit__(self, *exc):
+        n = len(STAGE_NAMES)
+        ms = (ctypes.c_double * n)()
+        cnt = (_LL * n)()
+        check(lib().lgb_profile_end(ms, cnt, n), "lgb_profile_end")
+        self.ms = {k: ms[i] for i, k in enumerate(STAGE_NAMES)}
+        self.launches = {k: int(cnt[i]) for i, k in enumerate(STAGE_NAMES)}
+        return False
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def lib():
+    """Load (once) and return the CUDA library; raise if it was never built."""
+    global _LIB
+    with _LOCK:
+        if _LIB is None:
+            path = library_path()
+            if not os.path.exists(path):
+                raise RuntimeError(
+                    f"leopard_em_gb300 CUDA library not found at {path}; build it with "
+                    "`python -m leopard_em_gb300.build` (there is no CPU fallback)"
+                )
+            handle = ctypes.CDLL(path)
+            for name, (args, res) in _SIGNATURES.items():
+                fn = getattr(handle, name)
+                fn.argtypes = args
+                fn.restype = res
+            _LIB = handle
+    return _LIB
+
+
+def check(status: int, what: str) -> None:
+    """Turn a non-zero lgb_status into a Python exception."""
+    if status == LGB_OK:
+        return
+    msg = lib().lgb_status_string(status).decode()
+    if status in (LGB_ERR_INVALID_ARGUMENT, LGB_ERR_UNSUPPORTED_SIZE, LGB_ERR_WORKSPACE_TOO_SMALL):
+        raise ValueError(f"{what}: {msg} (status {status})")
+    raise RuntimeError(f"{what}: {msg} (status {status})")

@@ -1,0 +1,268 @@
+"""Drop-in ``core_match_template`` running on the GB300 CUDA kernels.
+
+Same positional/keyword arguments and returned keys as Leopard-EM's
+``leopard_em.backend.core_match_template.core_match_template``
+(backend/core_match_template.py:146-363).  One process, one GPU, one CUDA
+stream: the reference's worker processes, work queue and per-stream
+round-robin (core_match_template.py:283-327, cross_correlation.py:101-142)
+become one in-order sequence of fused kernels on the caller's current stream.
+
+Semantics kept from the reference:
+  * projective filters = ctf_filters * whitening (core_match_template.py:274);
+  * global search index cs*D*N + df*N + orientation (:458-466, :513-520);
+  * MIP update with strict '>' per orientation batch, first index wins inside
+    a batch (backend/utils.py:241-252);
+  * decode and z-score scaling of process_results.py:67-183, including the
+    "correlation_variance" key holding the standard deviation.
+Deliberate differences (documented in the design doc):
+  * sums and sums of squares accumulate in FP64 (reference: FP32);
+  * the last, partial orientation batch is indexed correctly (the reference
+    always builds a full-length index vector, :513-520).
+"""
+
+from __future__ import annotations
+
+import ctypes
+import warnings
+
+import torch
+
+from .._native import MatchProblem, check, lib
+
+
+def _single_cuda_device(device) -> torch.device:
+    if isinstance(device, (list, tuple)):
+        if len(device) != 1:
+            raise ValueError(
+                f"leopard_em_gb300 runs on exactly one GPU per call; got {len(device)} devices"
+            )
+        device = device[0]
+    device = torch.device(device)
+    if device.type != "cuda":
+        raise ValueError(f"leopard_em_gb300 needs a CUDA device, got {device}")
+    if device.index is None:
+        device = torch.device("cuda", torch.cuda.current_device())
+    return device
+
+
+def _ptr(t: torch.Tensor) -> int:
+    return t.data_ptr()
+
+
+class MatchTemplateSearch:
+    """Device state of one whole-orientation search over one micrograph.
+
+    Holds the device copies of the inputs, the projective-filter stack, the
+    kernels' workspace and the four statistics maps.  ``run(begin, end)``
+    correlates an orientation range (callers may split the range to report
+    progress); ``result()`` decodes and scales the maps.
+    """
+
+    def __init__(
+        self,
+        image_dft: torch.Tensor,
+        template_dft: torch.Tensor,
+        ctf_filters: torch.Tensor,
+        whitening_filter_template: torch.Tensor,
+        defocus_values: torch.Tensor,
+        pixel_values: torch.Tensor,
+        euler_angles: torch.Tensor,
+        device,
+        orientation_batch_size: int = 1,
+    ):
+        self.device = _single_cuda_device(device)
+        if image_dft.dim() != 2 or template_dft.dim() != 3:
+            raise ValueError("image_dft must be (H, W//2+1) and template_dft (d, d, d//2+1)")
+        H, wc_img = image_dft.shape
+        W = 2 * (wc_img - 1)
+        d = template_dft.shape[0]
+        if tuple(template_dft.shape) != (d, d, d // 2 + 1):
+            raise ValueError(f"template_dft must be cubic (d, d, d//2+1), got {tuple(template_dft.shape)}")
+        n_cs, n_df = int(pixel_values.shape[0]), int(defocus_values.shape[0])
+        if tuple(ctf_filters.shape) != (n_cs, n_df, d, d // 2 + 1):
+            raise ValueError(
+                f"ctf_filters must be (num_Cs={n_cs}, num_defocus={n_df}, {d}, {d // 2 + 1}), "
+                f"got {tuple(ctf_filters.shape)}"
+            )
+        if tuple(whitening_filter_template.shape) != (d, d // 2 + 1):
+            raise ValueError("whitening_filter_template must be (d, d//2+1)")
+        if euler_angles.dim() != 2 or euler_angles.shape[1] != 3:
+            raise ValueError("euler_angles must be (N, 3)")
+        if orientation_batch_size < 1:
+            raise ValueError("orientation_batch_size must be >= 1")
+        self.problem = MatchProblem(
+            image_h=H,
+            image_w=W,
+            template_size=d,
+            n_pixel_sizes=n_cs,
+            n_defocus=n_df,
+            n_orientations=int(euler_angles.shape[0]),
+            orientation_batch=int(orientation_batch_size),
+        )
+        L = lib()
+        if not L.lgb_match_supported(ctypes.byref(self.problem)):
+            raise ValueError(
+                f"unsupported search shape: image {H}x{W}, template {d} (FFT lengths outside the compiled set)"
+            )
+        dev = self.device
+        with torch.cuda.device(dev):
+            stream = torch.cuda.current_stream(dev)
+            self._stream = stream
+            s = ctypes.c_void_p(stream.cuda_stream)
+            self.image_dft = image_dft.to(dev, torch.complex64, non_blocking=True).contiguous()
+            self.template_dft = template_dft.to(dev, torch.complex64, non_blocking=True).contiguous()
+            self.euler_angles = euler_angles.to(dev, torch.float32, non_blocking=True).contiguous()
+            self.defocus_values = defocus_values.to(dev, torch.float32, non_blocking=True).contiguous()
+            self.pixel_values = pixel_values.to(dev, torch.float32)
+            ctf = ctf_filters.to(dev, torch.float32, non_blocking=True).contiguous()
+            wf = whitening_filter_template.to(dev, torch.float32, non_blocking=True).contiguous()
+            self.projective_filters = torch.empty_like(ctf)
+            check(
+                L.lgb_match_filters(ctypes.byref(self.problem), _ptr(ctf), _ptr(wf), _ptr(self.projective_filters), s),
+                "lgb_match_filters",
+            )
+            nbytes = ctypes.c_size_t(0)
+            check(L.lgb_match_workspace_size(ctypes.byref(self.problem), ctypes.byref(nbytes)), "workspace size")
+            self.workspace = torch.empty(int(nbytes.value), dtype=torch.uint8, device=dev)
+            self.mip = torch.empty((H, W), dtype=torch.float32, device=dev)
+            self.best_index = torch.empty((H, W), dtype=torch.int32, device=dev)
+            self.corr_sum = torch.empty((H, W), dtype=torch.float64, device=dev)
+            self.corr_sq_sum = torch.empty((H, W), dtype=torch.float64, device=dev)
+            check(
+                L.lgb_match_init_stats(
+                    H * W, _ptr(self.mip), _ptr(self.best_index), _ptr(self.corr_sum), _ptr(self.corr_sq_sum), s
+                ),
+                "lgb_match_init_stats",
+            )
+            check(
+                L.lgb_match_prepare_image(
+                    ctypes.byref(self.problem), _ptr(self.image_dft), _ptr(self.workspace), self.workspace.numel(), s
+                ),
+                "lgb_match_prepare_image",
+            )
+        self.shape = (H, W)
+        self.orientations_done = 0
+
+    @property
+    def total_projections(self) -> int:
+        p = self.problem
+        return p.n_orientations * p.n_defocus * p.n_pixel_sizes
+
+    def run(self, begin: int = 0, end: int | None = None) -> None:
+        """Correlate orientations [begin, end) and fold them into the maps."""
+        end = self.problem.n_orientations if end is None else end
+        if not 0 <= begin <= end <= self.problem.n_orientations:
+            raise ValueError(f"orientation range [{begin}, {end}) outside [0, {self.problem.n_orientations})")
+        with torch.cuda.device(self.device):
+            s = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+            check(
+                lib().lgb_match_search(
+                    ctypes.byref(self.problem),
+                    _ptr(self.template_dft),
+                    _ptr(self.projective_filters),
+                    _ptr(self.euler_angles),
+                    int(begin),
+                    int(end),
+                    _ptr(self.mip),
+                    _ptr(self.best_index),
+                    _ptr(self.corr_sum),
+                    _ptr(self.corr_sq_sum),
+                    _ptr(self.workspace),
+                    self.workspace.numel(),
+                    s,
+                ),
+                "lgb_match_search",
+            )
+        self.orientations_done += end - begin
+
+    def result(self, to_cpu: bool = True) -> dict:
+        """Decode indices and compute mean / std / z-score (process_results.py:67-183)."""
+        H, W = self.shape
+        dev = self.device
+        with torch.cuda.device(dev):
+            s = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+            out = {k: torch.empty((H, W), dtype=torch.float32, device=dev) for k in
+                   ("scaled_mip", "best_phi", "best_theta", "best_psi", "best_defocus",
+                    "correlation_mean", "correlation_variance")}
+            check(
+                lib().lgb_match_finalize(
+                    ctypes.byref(self.problem),
+                    self.total_projections,
+                    _ptr(self.mip),
+                    _ptr(self.best_index),
+                    _ptr(self.corr_sum),
+                    _ptr(self.corr_sq_sum),
+                    _ptr(self.euler_angles),
+                    _ptr(self.defocus_values),
+                    _ptr(out["scaled_mip"]),
+                    _ptr(out["best_phi"]),
+                    _ptr(out["best_theta"]),
+                    _ptr(out["best_psi"]),
+                    _ptr(out["best_defocus"]),
+                    _ptr(out["correlation_mean"]),
+                    _ptr(out["correlation_variance"]),
+                    s,
+                ),
+                "lgb_match_finalize",
+            )
+            res = {
+                "mip": self.mip.clone(),
+                "scaled_mip": out["scaled_mip"],
+                "best_phi": out["best_phi"],
+                "best_theta": out["best_theta"],
+                "best_psi": out["best_psi"],
+                "best_defocus": out["best_defocus"],
+                "correlation_mean": out["correlation_mean"],
+                "correlation_variance": out["correlation_variance"],
+            }
+            if to_cpu:
+                res = {k: v.cpu() for k, v in res.items()}
+        res["total_projections"] = self.total_projections
+        res["total_orientations"] = self.problem.n_orientations
+        res["total_defocus"] = self.problem.n_defocus
+        return res
+
+
+def core_match_template(
+    image_dft: torch.Tensor,
+    template_dft: torch.Tensor,
+    ctf_filters: torch.Tensor,
+    whitening_filter_template: torch.Tensor,
+    defocus_values: torch.Tensor,
+    pixel_values: torch.Tensor,
+    euler_angles: torch.Tensor,
+    device: torch.device | list[torch.device],
+    orientation_batch_size: int = 1,
+    num_cuda_streams: int = 1,
+    backend: str = "streamed",
+    mag_matrix: torch.Tensor | None = None,
+) -> dict:
+    """Whole-orientation 2DTM search; see leopard_em.backend.core_match_template.
+
+    ``num_cuda_streams`` and ``backend`` are accepted for compatibility: both of
+    the reference's backends compute the same correlograms, and here they map to
+    the same fused kernel sequence on one stream.  Returns CPU tensors.
+    """
+    if backend not in ("streamed", "batched"):
+        raise ValueError(f"backend must be 'streamed' or 'batched', got {backend!r}")
+    if mag_matrix is not None:
+        raise ValueError("anisotropic magnification (mag_matrix) is not supported by leopard_em_gb300")
+    if num_cuda_streams > 1:
+        warnings.warn(
+            "num_cuda_streams is ignored: leopard_em_gb300 runs the search as one fused kernel "
+            "sequence on the current CUDA stream",
+            stacklevel=2,
+        )
+    search = MatchTemplateSearch(
+        image_dft,
+        template_dft,
+        ctf_filters,
+        whitening_filter_template,
+        defocus_values,
+        pixel_values,
+        euler_angles,
+        device,
+        orientation_batch_size,
+    )
+    search.run()
+    return search.result(to_cpu=True)

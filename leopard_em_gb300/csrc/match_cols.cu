@@ -1,0 +1,57 @@
+// Launcher: the fused column pass (forward FFT, cross power, inverse FFT) for
+// image height H.
+#include "match_kernels.cuh"
+#include "match_launch.h"
+
+namespace lgb {
+
+#define LGB_COL_SIZES(X) X(48) X(64) X(128) X(256) X(288) X(512) X(576) X(1024) X(2048) X(4096)
+
+bool supported_col(int H) {
+  switch (H) {
+#define X(n) case n:
+    LGB_COL_SIZES(X)
+#undef X
+    return true;
+    default:
+      return false;
+  }
+}
+
+template <int HN>
+static int colpass_t(const void* A, const void* Ip, int h, int Wcp, int n_c, void* Y, cudaStream_t s) {
+  constexpr int NT = FftThreads<HN>::value;
+  const size_t smem = sizeof(float2) * kColGroup * (IdxPad16::pad(HN) + 4);
+  if (cudaFuncSetAttribute(colpass_kernel<HN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return LGB_ERR_CUDA;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int groups = Wcp / kColGroup;
+  // split the correlogram loop so that the grid covers at least ~4 waves
+  int split = 1;
+  while (split < n_c && groups * split < 4 * sms) split *= 2;
+  if (split > n_c) split = n_c;
+  const int per = (n_c + split - 1) / split;
+  split = (n_c + per - 1) / per;
+  dim3 grid(groups, split);
+  colpass_kernel<HN><<<grid, kColGroup * NT, smem, s>>>(static_cast<const float2*>(A),
+                                                       static_cast<const float2*>(Ip), h, Wcp, n_c, per,
+                                                       static_cast<float2*>(Y));
+  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+}
+
+int launch_colpass(int H, const void* A, const void* Ip, int h, int Wcp, int n_c, void* Y, cudaStream_t s) {
+  switch (H) {
+#define X(n) \
+  case n:    \
+    return colpass_t<n>(A, Ip, h, Wcp, n_c, Y, s);
+    LGB_COL_SIZES(X)
+#undef X
+    default:
+      return LGB_ERR_UNSUPPORTED_SIZE;
+  }
+}
+
+}  // namespace lgb

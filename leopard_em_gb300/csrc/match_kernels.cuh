@@ -1,0 +1,380 @@
+// Kernels of the plain FP32 whole-orientation search.
+//
+// Per orientation batch (B orientations, C*D projective filters, n_c = C*D*B
+// correlograms, c = (cs*D + df)*B + b):
+//   slice_kernel      Fourier slice of the template at R(phi,theta,psi),
+//                     rows un-shifted, DC zeroed, contrast flipped
+//                     (cross_correlation.py:76-92)                     [B, d, d/2+1]
+//   proj_col_kernel   x projective filter, inverse FFT along y          [n_c, d, d/2+1]
+//   proj_row_kernel   c2r along x, 1/d^2, ifftshift, per-row moments    [n_c, d, d]
+//   pad_rfft_kernel   edge-mean/variance normalisation (utils.py:106-188)
+//                     and the zero-padded row rfft of length W          [n_c, d, Wcp]
+//   colpass_kernel    per column: pruned FFT along y (length H), cross power
+//                     image * conj(P) with P[0,0]=0, inverse FFT along y
+//                                                                      [n_c, H, Wcp]
+//   rowpass_kernel    per row: c2r of length W (1/(H W)) and the fused
+//                     statistics update (utils.py:191-255): max over the
+//                     batch, strict '>' MIP update, global index, FP64 sums
+#pragma once
+
+#include "fft.cuh"
+
+namespace lgb {
+
+constexpr int kColGroup = 4;  // columns per colpass CTA: 4 x 8 B = one 32 B sector per row
+
+__host__ __device__ inline int pad4(int n) { return (n + 3) & ~3; }
+
+// ---------------------------------------------------------------------------
+// Euler (ZYZ, degrees) -> R = Rz(phi) Ry(theta) Rz(psi), in FP64.
+// ---------------------------------------------------------------------------
+__device__ inline void euler_zyz_to_rotmat(const float* e, float* R) {
+  const double k = 3.14159265358979323846 / 180.0;
+  double sp, cp, st, ct, ss, cs;
+  sincos((double)e[0] * k, &sp, &cp);
+  sincos((double)e[1] * k, &st, &ct);
+  sincos((double)e[2] * k, &ss, &cs);
+  R[0] = (float)(cp * ct * cs - sp * ss);
+  R[1] = (float)(-cp * ct * ss - sp * cs);
+  R[2] = (float)(cp * st);
+  R[3] = (float)(sp * ct * cs + cp * ss);
+  R[4] = (float)(-sp * ct * ss + cp * cs);
+  R[5] = (float)(sp * st);
+  R[6] = (float)(-st * cs);
+  R[7] = (float)(st * ss);
+  R[8] = (float)ct;
+}
+
+// ---------------------------------------------------------------------------
+// proj_col: T[c][y][kx] = IFFT_y( slice_b[y][kx] * pf[cd][y][kx] )   (unscaled)
+// ---------------------------------------------------------------------------
+template <int HT, int COLS>
+__global__ void __launch_bounds__(COLS* FftThreads<HT>::value)
+    proj_col_kernel(const float2* __restrict__ slices, const float* __restrict__ pf, int nb,
+                    float2* __restrict__ T) {
+  constexpr int NT = FftThreads<HT>::value;
+  constexpr int WC = HT / 2 + 1;
+  constexpr int STRIDE = IdxPad16::pad(HT) + 2;
+  __shared__ float2 buf[COLS * STRIDE];
+  const int c = blockIdx.y;
+  const int cd = c / nb, b = c - (c / nb) * nb;
+  const int kx0 = blockIdx.x * COLS;
+  const float2* sl = slices + (size_t)b * HT * WC;
+  const float* f = pf + (size_t)cd * HT * WC;
+  for (int e = threadIdx.x; e < HT * COLS; e += blockDim.x) {
+    const int y = e / COLS, i = e % COLS, kx = kx0 + i;
+    float2 v = make_float2(0.f, 0.f);
+    if (kx < WC) {
+      v = sl[y * WC + kx];
+      const float w = f[y * WC + kx];
+      v.x *= w;
+      v.y *= w;
+    }
+    buf[i * STRIDE + IdxPad16::f(y)] = v;
+  }
+  __syncthreads();
+  const int g = threadIdx.x / NT, t = threadIdx.x - (threadIdx.x / NT) * NT;
+  block_fft<HT, NT, +1, IdxPad16>(buf + g * STRIDE, t);
+  float2* out = T + (size_t)c * HT * WC;
+  for (int e = threadIdx.x; e < HT * COLS; e += blockDim.x) {
+    const int y = e / COLS, i = e % COLS, kx = kx0 + i;
+    if (kx < WC) out[y * WC + kx] = buf[i * STRIDE + IdxPad16::f(y)];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// proj_row: c2r along x of each row of T[c] (length HT via an HT/2 complex
+// inverse FFT), scale 1/HT^2, ifftshift both axes, and per-row moments
+// rowstats[c][py] = (sum, sum of squares, edge sum) in FP64.
+// Imaginary parts of the DC and Nyquist bins are ignored (c2r convention).
+// ---------------------------------------------------------------------------
+template <int HT, int ROWS>
+__global__ void __launch_bounds__(ROWS* FftThreads<HT / 2>::value)
+    proj_row_kernel(const float2* __restrict__ T, float* __restrict__ proj, double* __restrict__ rowstats) {
+  constexpr int M = HT / 2;
+  constexpr int WC = HT / 2 + 1;
+  constexpr int NT = FftThreads<M>::value;
+  constexpr int ZS = IdxPad16::pad(M) + 2;
+  __shared__ float2 xin[ROWS][WC];
+  __shared__ float2 z[ROWS][ZS];
+  __shared__ double part[ROWS * NT][3];
+  const int c = blockIdx.y;
+  const int g = threadIdx.x / NT, t = threadIdx.x - (threadIdx.x / NT) * NT;
+  const int row0 = blockIdx.x * ROWS;
+  const float2* src = T + ((size_t)c * HT + row0) * WC;
+  for (int e = threadIdx.x; e < ROWS * WC; e += blockDim.x) xin[e / WC][e % WC] = src[e];
+  __syncthreads();
+  for (int k = t; k < M; k += NT) {
+    float2 A = xin[g][k];
+    float2 B = xin[g][M - k];
+    if (k == 0) { A.y = 0.f; B.y = 0.f; }  // DC and Nyquist: real parts only
+    B.y = -B.y;                            // conj
+    const float2 xe = cadd(A, B);
+    float s, co;
+    sincospif(2.0f * (float)k / (float)HT, &s, &co);
+    const float2 xo = cmul(csub(A, B), make_float2(co, s));
+    z[g][IdxPad16::f(k)] = cadd(xe, mul_i<1>(xo));
+  }
+  __syncthreads();
+  block_fft<M, NT, +1, IdxPad16>(z[g], t);
+  const int y = row0 + g;
+  const int py = (y + HT - HT / 2) % HT;
+  const float scale = 1.0f / ((float)HT * (float)HT);
+  const bool edge_row = (py == 0) || (py == HT - 1);
+  double s1 = 0.0, s2 = 0.0, se = 0.0;
+  float* prow = proj + ((size_t)c * HT + py) * HT;
+  for (int m = t; m < M; m += NT) {
+    const float2 v = z[g][IdxPad16::f(m)];
+    const float a = v.x * scale, b = v.y * scale;
+    const int px0 = (2 * m + HT - HT / 2) % HT, px1 = (2 * m + 1 + HT - HT / 2) % HT;
+    prow[px0] = a;
+    prow[px1] = b;
+    s1 += (double)a + (double)b;
+    s2 += (double)a * a + (double)b * b;
+    if (edge_row) {
+      se += (double)a + (double)b;
+    } else {
+      if (px0 == 0 || px0 == HT - 1) se += a;
+      if (px1 == 0 || px1 == HT - 1) se += b;
+    }
+  }
+  part[threadIdx.x][0] = s1;
+  part[threadIdx.x][1] = s2;
+  part[threadIdx.x][2] = se;
+  __syncthreads();
+  if (t == 0) {
+    double a = 0, b = 0, e = 0;
+    for (int i = 0; i < NT; ++i) {
+      a += part[g * NT + i][0];
+      b += part[g * NT + i][1];
+      e += part[g * NT + i][2];
+    }
+    double* rs = rowstats + ((size_t)c * HT + py) * 3;
+    rs[0] = a;
+    rs[1] = b;
+    rs[2] = e;
+  }
+}
+
+// Normalisation constants of utils.py:106-188 from the per-row moments:
+// returns edge mean e and scale s such that normalised = (p - e) * s.
+__device__ inline void projection_norm_constants(const double* rs, int h, int H, int W, float* e_out,
+                                                 float* s_out) {
+  // warp 0 reduces h rows
+  double s1 = 0, s2 = 0, se = 0;
+  const int lane = threadIdx.x & 31;
+  for (int r = lane; r < h; r += 32) {
+    s1 += rs[3 * r];
+    s2 += rs[3 * r + 1];
+    se += rs[3 * r + 2];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    s2 += __shfl_down_sync(0xffffffffu, s2, o);
+    se += __shfl_down_sync(0xffffffffu, se, o);
+  }
+  if (lane == 0) {
+    const double n = (double)h * (double)h;
+    const double e = se / (double)(4 * h - 4);
+    const double S1 = s1 - n * e;                  // sum of (p - e)
+    const double S2 = s2 - 2.0 * e * s1 + n * e * e;  // sum of (p - e)^2
+    const double rel = n / ((double)H * (double)W);
+    const double mean = (S1 / n) * rel * rel;
+    double var = S2 - 2.0 * mean * S1 + n * mean * mean;
+    var += (double)(H - h) * (double)(W - h) * mean * mean;
+    if (var < 1e-8) var = 1e-8;
+    *e_out = (float)e;
+    *s_out = (float)(sqrt((double)H * (double)W) / sqrt(var));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// pad_rfft: A[c][y][k] = rfft_W( normalised projection row y, zero padded )
+// for k = 0..W/2, zeros up to Wcp.  Real FFT of length W = 2*WH through a
+// WH-point complex FFT (first pass pruned to the ceil(h/2) non-zero inputs).
+// ---------------------------------------------------------------------------
+template <int WH, int ROWS>
+__global__ void __launch_bounds__(ROWS* FftThreads<WH>::value)
+    pad_rfft_kernel(const float* __restrict__ proj, const double* __restrict__ rowstats, int h, int H,
+                    int Wcp, float2* __restrict__ A) {
+  constexpr int NT = FftThreads<WH>::value;
+  constexpr int ZS = IdxPad16::pad(WH) + 2;
+  __shared__ float2 z[ROWS][ZS];
+  __shared__ float norm[2];
+  const int c = blockIdx.y;
+  const int W = 2 * WH;
+  if (threadIdx.x < 32) projection_norm_constants(rowstats + (size_t)c * h * 3, h, H, W, &norm[0], &norm[1]);
+  __syncthreads();
+  const float e = norm[0], s = norm[1];
+  const int g = threadIdx.x / NT, t = threadIdx.x - (threadIdx.x / NT) * NT;
+  const int y = blockIdx.x * ROWS + g;
+  const bool active = y < h;
+  const int nz = (h + 1) / 2;
+  if (active) {
+    const float* p = proj + ((size_t)c * h + y) * h;
+    for (int m = t; m < nz; m += NT) {
+      const float a = (p[2 * m] - e) * s;
+      const float b = (2 * m + 1 < h) ? (p[2 * m + 1] - e) * s : 0.f;
+      z[g][IdxPad16::f(m)] = make_float2(a, b);
+    }
+  }
+  __syncthreads();
+  block_fft_pruned<WH, NT, -1, IdxPad16>(z[g], t, nz);
+  if (!active) return;
+  float2* out = A + ((size_t)c * h + y) * Wcp;
+  for (int k = t; k <= WH; k += NT) {
+    const float2 Zk = z[g][IdxPad16::f(k == WH ? 0 : k)];
+    const float2 Zm = cconj(z[g][IdxPad16::f(k == 0 ? 0 : WH - k)]);
+    const float2 xe = cscale(cadd(Zk, Zm), 0.5f);
+    const float2 xo = mul_i<-1>(cscale(csub(Zk, Zm), 0.5f));
+    float sn, cs;
+    sincospif((float)k / (float)WH, &sn, &cs);
+    out[k] = cadd(xe, cmul(make_float2(cs, -sn), xo));
+  }
+  for (int k = WH + 1 + t; k < Wcp; k += NT) out[k] = make_float2(0.f, 0.f);
+}
+
+// ---------------------------------------------------------------------------
+// colpass: per group of 4 columns, for each correlogram c in this CTA's range:
+//   P = FFT_y(A_c[0..h), zero padded to HN);  X = I * conj(P), X[0,0] = 0;
+//   Y_c = IFFT_y(X)   (unscaled)
+// ---------------------------------------------------------------------------
+template <int HN>
+__global__ void __launch_bounds__(kColGroup* FftThreads<HN>::value, 1)
+    colpass_kernel(const float2* __restrict__ A, const float2* __restrict__ Ip, int h, int Wcp, int n_c,
+                   int c_per_block, float2* __restrict__ Y) {
+  constexpr int NT = FftThreads<HN>::value;
+  constexpr int STRIDE = IdxPad16::pad(HN) + 4;
+  extern __shared__ float2 cbuf[];
+  const int kx0 = blockIdx.x * kColGroup;
+  const int c_begin = blockIdx.y * c_per_block;
+  const int c_end = min(n_c, c_begin + c_per_block);
+  const int g = threadIdx.x / NT, t = threadIdx.x - (threadIdx.x / NT) * NT;
+  constexpr int NTH = kColGroup * NT;
+#pragma unroll 1
+  for (int c = c_begin; c < c_end; ++c) {
+    const float2* a = A + (size_t)c * h * Wcp + kx0;
+#pragma unroll 1
+    for (int e = threadIdx.x; e < h * kColGroup; e += NTH) {
+      const int y = e / kColGroup, i = e % kColGroup;
+      cbuf[i * STRIDE + IdxPad16::f(y)] = a[(size_t)y * Wcp + i];
+    }
+    __syncthreads();
+    block_fft_pruned_outline<HN, NT, -1, IdxPad16>(cbuf + g * STRIDE, t, h);
+#pragma unroll 2
+    for (int e = threadIdx.x; e < HN * kColGroup; e += NTH) {
+      const int y = e / kColGroup, i = e % kColGroup;
+      const float2 I = __ldg(Ip + (size_t)y * Wcp + kx0 + i);
+      const int si = i * STRIDE + IdxPad16::f(y);
+      float2 X = cmulc(I, cbuf[si]);
+      if (y == 0 && kx0 + i == 0) X = make_float2(0.f, 0.f);
+      cbuf[si] = X;
+    }
+    __syncthreads();
+    block_fft_outline<HN, NT, +1, IdxPad16>(cbuf + g * STRIDE, t);
+    float2* yo = Y + (size_t)c * HN * Wcp + kx0;
+#pragma unroll 2
+    for (int e = threadIdx.x; e < HN * kColGroup; e += NTH) {
+      const int y = e / kColGroup, i = e % kColGroup;
+      yo[(size_t)y * Wcp + i] = cbuf[i * STRIDE + IdxPad16::f(y)];
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// rowpass: row y of every correlogram in the batch: c2r of length W = 2*WH
+// (imaginary parts of DC / Nyquist ignored), scale 1/(H W), then the fused
+// statistics update of utils.py:191-255 (max over the batch in c order with
+// strict '>', MIP update with strict '>', global index, FP64 sums).
+// ---------------------------------------------------------------------------
+constexpr int kRowThreads = 256;
+
+// Largest divisor of WH that is <= kRowThreads (threads of one rowpass CTA).
+constexpr int row_threads(int wh, int cand = kRowThreads) {
+  return cand <= 1 ? 1 : (wh % cand == 0 ? cand : row_threads(wh, cand - 1));
+}
+
+template <int WH, int NT>
+__global__ void __launch_bounds__(NT, 2)
+    rowpass_kernel(const float2* __restrict__ Y, int H, int Wcp, int n_c, int nb, int n_orient, int o0,
+                   float scale, float* __restrict__ mip, int* __restrict__ best, double* __restrict__ s1,
+                   double* __restrict__ s2) {
+  static_assert(NT >= FftThreads<WH>::value, "row FFT needs more threads");
+  static_assert(WH % NT == 0, "row length must be a multiple of the CTA size");
+  constexpr int PIX = WH / NT;
+  constexpr int ZS = IdxPad16::pad(WH) + 2;
+  __shared__ float2 xr[WH + 4];
+  __shared__ float2 z[ZS];
+  const int y = blockIdx.x;
+  const int t = threadIdx.x;
+  float bmax[2 * PIX], bs[2 * PIX], bss[2 * PIX];
+  int barg[2 * PIX];
+#pragma unroll
+  for (int i = 0; i < 2 * PIX; ++i) {
+    bmax[i] = -INFINITY;
+    barg[i] = 0;
+    bs[i] = 0.f;
+    bss[i] = 0.f;
+  }
+  for (int c = 0; c < n_c; ++c) {
+    const float2* row = Y + ((size_t)c * H + y) * Wcp;
+    for (int k = t; k <= WH; k += NT) xr[k] = row[k];
+    __syncthreads();
+    for (int k = t; k < WH; k += NT) {
+      float2 A = xr[k];
+      float2 B = xr[WH - k];
+      if (k == 0) { A.y = 0.f; B.y = 0.f; }
+      B.y = -B.y;
+      const float2 xe = cadd(A, B);
+      float sn, cs;
+      sincospif((float)k / (float)WH, &sn, &cs);
+      const float2 xo = cmul(csub(A, B), make_float2(cs, sn));
+      z[IdxPad16::f(k)] = cadd(xe, mul_i<1>(xo));
+    }
+    __syncthreads();
+    block_fft_outline<WH, NT, +1, IdxPad16>(z, t);
+#pragma unroll
+    for (int r = 0; r < PIX; ++r) {
+      const float2 v = z[IdxPad16::f(t + r * NT)];
+      const float a = v.x * scale, b = v.y * scale;
+      if (a > bmax[2 * r]) { bmax[2 * r] = a; barg[2 * r] = c; }
+      if (b > bmax[2 * r + 1]) { bmax[2 * r + 1] = b; barg[2 * r + 1] = c; }
+      bs[2 * r] += a;
+      bss[2 * r] = fmaf(a, a, bss[2 * r]);
+      bs[2 * r + 1] += b;
+      bss[2 * r + 1] = fmaf(b, b, bss[2 * r + 1]);
+    }
+    __syncthreads();
+  }
+  const size_t W = 2 * (size_t)WH;
+#pragma unroll
+  for (int r = 0; r < PIX; ++r) {
+    const size_t idx = (size_t)y * W + 2 * (size_t)(t + r * NT);
+    float2 m = *reinterpret_cast<float2*>(mip + idx);
+    int2 bi = *reinterpret_cast<int2*>(best + idx);
+    double2 a = *reinterpret_cast<double2*>(s1 + idx);
+    double2 q = *reinterpret_cast<double2*>(s2 + idx);
+    if (bmax[2 * r] > m.x) {
+      m.x = bmax[2 * r];
+      const int cc = barg[2 * r];
+      bi.x = (cc / nb) * n_orient + o0 + (cc - (cc / nb) * nb);
+    }
+    if (bmax[2 * r + 1] > m.y) {
+      m.y = bmax[2 * r + 1];
+      const int cc = barg[2 * r + 1];
+      bi.y = (cc / nb) * n_orient + o0 + (cc - (cc / nb) * nb);
+    }
+    a.x += (double)bs[2 * r];
+    a.y += (double)bs[2 * r + 1];
+    q.x += (double)bss[2 * r];
+    q.y += (double)bss[2 * r + 1];
+    *reinterpret_cast<float2*>(mip + idx) = m;
+    *reinterpret_cast<int2*>(best + idx) = bi;
+    *reinterpret_cast<double2*>(s1 + idx) = a;
+    *reinterpret_cast<double2*>(s2 + idx) = q;
+  }
+}
+
+}  // namespace lgb

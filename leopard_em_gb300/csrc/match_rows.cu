@@ -1,0 +1,71 @@
+// Launchers: zero-padded projection rfft and the row c2r + statistics pass
+// (image width W).
+#include "match_kernels.cuh"
+#include "match_launch.h"
+
+namespace lgb {
+
+// W/2 values
+#define LGB_ROW_SIZES(X) X(32) X(40) X(64) X(128) X(144) X(256) X(288) X(512) X(1024) X(2048)
+
+bool supported_row(int W) {
+  if (W % 2) return false;
+  switch (W / 2) {
+#define X(n) case n:
+    LGB_ROW_SIZES(X)
+#undef X
+    return true;
+    default:
+      return false;
+  }
+}
+
+template <int WH>
+static int pad_rfft_t(const float* proj, const double* rowstats, int h, int H, int Wcp, int n_c, void* A,
+                      cudaStream_t s) {
+  constexpr int NT = FftThreads<WH>::value;
+  constexpr int ROWS = NT >= 128 ? 2 : (NT >= 32 ? 4 : 8);
+  dim3 grid((h + ROWS - 1) / ROWS, n_c);
+  pad_rfft_kernel<WH, ROWS><<<grid, ROWS * NT, 0, s>>>(proj, rowstats, h, H, Wcp, static_cast<float2*>(A));
+  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+}
+
+template <int WH>
+static int rowpass_t(const void* Y, int H, int Wcp, int n_c, int nb, int n_orient, int o0, float* mip, int* best,
+                     double* s1, double* s2, cudaStream_t s) {
+  constexpr int NT = row_threads(WH);
+  const float scale = 1.0f / ((float)H * (float)(2 * WH));
+  rowpass_kernel<WH, NT><<<H, NT, 0, s>>>(static_cast<const float2*>(Y), H, Wcp, n_c, nb, n_orient, o0, scale, mip,
+                                          best, s1, s2);
+  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+}
+
+int launch_pad_rfft(int W, const float* proj, const double* rowstats, int h, int H, int Wcp, int n_c, void* A,
+                    cudaStream_t s) {
+  if (W % 2) return LGB_ERR_UNSUPPORTED_SIZE;
+  switch (W / 2) {
+#define X(n) \
+  case n:    \
+    return pad_rfft_t<n>(proj, rowstats, h, H, Wcp, n_c, A, s);
+    LGB_ROW_SIZES(X)
+#undef X
+    default:
+      return LGB_ERR_UNSUPPORTED_SIZE;
+  }
+}
+
+int launch_rowpass(int W, const void* Y, int H, int Wcp, int n_c, int nb, int n_orient, int o0, float* mip,
+                   int* best, double* s1, double* s2, cudaStream_t s) {
+  if (W % 2) return LGB_ERR_UNSUPPORTED_SIZE;
+  switch (W / 2) {
+#define X(n) \
+  case n:    \
+    return rowpass_t<n>(Y, H, Wcp, n_c, nb, n_orient, o0, mip, best, s1, s2, s);
+    LGB_ROW_SIZES(X)
+#undef X
+    default:
+      return LGB_ERR_UNSUPPORTED_SIZE;
+  }
+}
+
+}  // namespace lgb

@@ -1,0 +1,147 @@
+"""Host-side preparation of the search inputs (CPU torch, once per micrograph).
+
+These mirror what ``MatchTemplateManager.make_backend_core_function_kwargs``
+does before calling the backend (match_template_manager.py:140-218):
+  * ``volume_to_rfft_fourier_slice``  utils/image_processing.py:179-202
+  * ``preprocess_image``              utils/image_processing.py:16-75
+  * ``ctf_2d`` / ``ctf_filter_stack`` utils/ctf_utils.py:19-116, with the
+    published CTF formula (the reference calls torch-ctf's calculate_ctf_2d)
+  * ``get_cs_range``                  utils/search_utils.py:6-29
+  * ``whitening_filter``              a radially averaged 1/sqrt(power) filter,
+    the published construction of torch-fourier-filter's whitening_filter.
+They are not part of the timed search.
+"""
+
+from __future__ import annotations
+
+import math
+
+import torch
+
+
+def volume_to_rfft_fourier_slice(volume: torch.Tensor) -> torch.Tensor:
+    """fftshift -> rfftn -> fftshift over the first two axes."""
+    if volume.dim() != 3:
+        raise ValueError("volume must be 3D")
+    v = torch.fft.fftshift(volume, dim=(0, 1, 2))
+    v = torch.fft.rfftn(v, dim=(0, 1, 2))
+    return torch.fft.fftshift(v, dim=(0, 1))
+
+
+def preprocess_image(image_rfft, cumulative_fourier_filters, bandpass_filter, full_image_shape, extracted_box_shape):
+    """Filter, normalise to unit power, scale by sqrt(dimensionality) and box area."""
+    image_rfft = image_rfft * cumulative_fourier_filters
+    sq = torch.abs(image_rfft) ** 2
+    ssum = torch.sum(sq, dim=(-2, -1), keepdim=True)
+    ssum = ssum + torch.sum(sq[..., :, 1:-1], dim=(-2, -1), keepdim=True)
+    image_rfft = image_rfft / torch.sqrt(ssum)
+    dimensionality = bandpass_filter.sum() + bandpass_filter[:, 1:-1].sum()
+    image_rfft = image_rfft * dimensionality**0.5
+    img_h, img_w = full_image_shape
+    box_h, box_w = extracted_box_shape
+    return image_rfft * ((img_h * img_w) / (box_h * box_w)) ** 0.5
+
+
+def rfft_freq_grid(shape: tuple[int, int], pixel_size: float = 1.0):
+    """(ky, kx) spatial frequencies (1/Angstrom) of an unshifted rfft grid."""
+    h, w = shape
+    ky = torch.fft.fftfreq(h, dtype=torch.float64)[:, None] / pixel_size
+    kx = torch.fft.rfftfreq(w, dtype=torch.float64)[None, :] / pixel_size
+    return ky.expand(h, w // 2 + 1), kx.expand(h, w // 2 + 1)
+
+
+def electron_wavelength(voltage_kv: float) -> float:
+    """Relativistic electron wavelength in Angstrom."""
+    v = voltage_kv * 1e3
+    h, m0, e, c = 6.62607015e-34, 9.1093837015e-31, 1.602176634e-19, 299792458.0
+    return h / math.sqrt(2 * m0 * e * v * (1 + e * v / (2 * m0 * c * c))) * 1e10
+
+
+def ctf_2d(
+    shape: tuple[int, int],
+    defocus: float,
+    astigmatism: float = 0.0,
+    astigmatism_angle: float = 0.0,
+    voltage: float = 300.0,
+    spherical_aberration: float = 2.7,
+    amplitude_contrast: float = 0.07,
+    phase_shift: float = 0.0,
+    pixel_size: float = 1.0,
+    b_factor: float = 0.0,
+) -> torch.Tensor:
+    """CTF on an unshifted rfft grid: -sin(chi), defocus/astigmatism in Angstrom.
+
+    chi = pi*lambda*k^2*df(theta) - pi/2*Cs*lambda^3*k^4 + phase + asin(A)-term,
+    with df(theta) = defocus + astigmatism*cos(2(theta - angle)), written in the
+    sign convention -sin(-pi lambda df k^2 + pi/2 Cs lambda^3 k^4 - phi - atan(A/sqrt(1-A^2))),
+    and an optional B-factor envelope exp(-B k^2 / 4).
+    """
+    ky, kx = rfft_freq_grid(shape, pixel_size)
+    k2 = kx**2 + ky**2
+    lam = electron_wavelength(voltage)
+    cs = spherical_aberration * 1e7
+    ang = torch.atan2(ky, kx)
+    df = defocus + astigmatism * torch.cos(2 * (ang - math.radians(astigmatism_angle)))
+    k5 = math.atan(amplitude_contrast / math.sqrt(1 - amplitude_contrast**2))
+    chi = -math.pi * lam * k2 * df + 0.5 * math.pi * cs * lam**3 * k2**2 - math.radians(phase_shift) - k5
+    out = -torch.sin(chi)
+    if b_factor:
+        out = out * torch.exp(-b_factor * k2 / 4)
+    return out.to(torch.float32)
+
+
+def get_cs_range(pixel_size: float, pixel_size_offsets: torch.Tensor, cs: float = 2.7) -> torch.Tensor:
+    """Cs values emulating relative pixel-size changes (search_utils.py:6-29)."""
+    return cs / torch.pow((pixel_size + pixel_size_offsets) / pixel_size, 4)
+
+
+def ctf_filter_stack(
+    template_size: int,
+    defocus_u: float,
+    defocus_v: float,
+    defocus_offsets: torch.Tensor,
+    pixel_size_offsets: torch.Tensor,
+    astigmatism_angle: float = 0.0,
+    voltage: float = 300.0,
+    spherical_aberration: float = 2.7,
+    amplitude_contrast: float = 0.07,
+    phase_shift: float = 0.0,
+    pixel_size: float = 1.0,
+    b_factor: float = 0.0,
+) -> torch.Tensor:
+    """(num_pixel_sizes, num_defocus, d, d//2+1) stack as ctf_utils.py:19-116."""
+    mean_df = (defocus_u + defocus_v) / 2
+    astig = abs(defocus_u - defocus_v) / 2
+    cs_values = get_cs_range(pixel_size, pixel_size_offsets, spherical_aberration)
+    stack = []
+    for cs in cs_values.tolist():
+        stack.append(
+            torch.stack(
+                [
+                    ctf_2d((template_size, template_size), mean_df + float(o), astig, astigmatism_angle, voltage, cs,
+                           amplitude_contrast, phase_shift, pixel_size, b_factor)
+                    for o in defocus_offsets.tolist()
+                ]
+            )
+        )
+    return torch.stack(stack)
+
+
+def whitening_filter(image_rfft: torch.Tensor, output_shape: tuple[int, int], num_bins: int | None = None):
+    """1/sqrt(radially averaged power) of ``image_rfft`` sampled on ``output_shape``
+    (an rfft grid of real shape output_shape), normalised to max 1."""
+    H = image_rfft.shape[-2]
+    W = 2 * (image_rfft.shape[-1] - 1)
+    ky, kx = rfft_freq_grid((H, W))
+    r = torch.sqrt(kx**2 + ky**2)
+    nb = num_bins or int(max(H, W) // 2 + 1)
+    idx = torch.clamp((r / 0.5 * (nb - 1)).round().long(), 0, nb - 1)
+    power = torch.zeros(nb, dtype=torch.float64).index_add_(0, idx.flatten(), (image_rfft.abs() ** 2).flatten().double())
+    count = torch.zeros(nb, dtype=torch.float64).index_add_(0, idx.flatten(), torch.ones(idx.numel(), dtype=torch.float64))
+    spec = torch.sqrt(power / count.clamp_min(1))
+    filt1d = torch.where(spec > 0, 1.0 / spec, torch.zeros_like(spec))
+    filt1d = filt1d / filt1d.max()
+    ky2, kx2 = rfft_freq_grid(output_shape)
+    r2 = torch.sqrt(kx2**2 + ky2**2)
+    idx2 = torch.clamp((r2 / 0.5 * (nb - 1)).round().long(), 0, nb - 1)
+    return filt1d[idx2].to(torch.float32)

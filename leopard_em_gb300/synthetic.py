@@ -1,0 +1,219 @@
+"""Seeded synthetic 2DTM workloads (stand-ins for the reference's benchmark data).
+
+Every configuration is built from one integer seed:
+  * template: a cubic volume that is a sum of isotropic Gaussian blobs
+    (exp(-|r-c|^2 / 2 sigma^2)) with centres uniform in a ball;
+  * micrograph: i.i.d. N(0,1) noise plus particles.  A particle is the exact
+    line-integral projection of the blob volume at rotation R (blob centre c
+    projects to (R^T c)_xy, the convention of the Fourier-slice search), CTF
+    filtered, scaled so that its variance over the d x d box is ``snr`` times
+    the noise variance, contrast inverted (the search flips the template
+    contrast) and added with its box's top-left corner at a random position;
+  * search inputs: preprocessed image spectrum, fftshifted template rfft, CTF
+    stack, whitening filter, defocus and pixel-size offsets, Euler grid.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import preprocess as pp
+
+
+def blob_volume(size: int, n_blobs: int, sigma: float, radius: float, seed: int, device="cpu"):
+    """Sum of Gaussian blobs; returns (volume[z,y,x] float32, centres (n,3) xyz
+    relative to voxel size//2)."""
+    rng = np.random.default_rng(seed)
+    # uniform in a ball
+    v = rng.normal(size=(n_blobs, 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    r = radius * rng.uniform(size=(n_blobs, 1)) ** (1.0 / 3.0)
+    centres = v * r
+    vol = torch.zeros((size, size, size), dtype=torch.float32, device=device)
+    half = size // 2
+    win = int(math.ceil(4 * sigma))
+    offs = torch.arange(-win, win + 1, device=device, dtype=torch.float32)
+    for cx, cy, cz in centres:
+        ix, iy, iz = int(round(cx)) + half, int(round(cy)) + half, int(round(cz)) + half
+        gx = torch.exp(-((offs + ix - half - cx) ** 2) / (2 * sigma**2))
+        gy = torch.exp(-((offs + iy - half - cy) ** 2) / (2 * sigma**2))
+        gz = torch.exp(-((offs + iz - half - cz) ** 2) / (2 * sigma**2))
+        blk = gz[:, None, None] * gy[None, :, None] * gx[None, None, :]
+        z0, y0, x0 = iz - win, iy - win, ix - win
+        zs, ys, xs = max(z0, 0), max(y0, 0), max(x0, 0)
+        ze, ye, xe = min(z0 + 2 * win + 1, size), min(y0 + 2 * win + 1, size), min(x0 + 2 * win + 1, size)
+        if ze <= zs or ye <= ys or xe <= xs:
+            continue
+        vol[zs:ze, ys:ye, xs:xe] += blk[zs - z0 : ze - z0, ys - y0 : ye - y0, xs - x0 : xe - x0]
+    return vol, centres
+
+
+def euler_zyz_from_rotmat(R: np.ndarray) -> np.ndarray:
+    """(phi, theta, psi) in degrees with R = Rz(phi) Ry(theta) Rz(psi)."""
+    theta = math.degrees(math.acos(max(-1.0, min(1.0, R[2, 2]))))
+    if abs(R[2, 2]) < 1 - 1e-9:
+        phi = math.degrees(math.atan2(R[1, 2], R[0, 2]))
+        psi = math.degrees(math.atan2(R[2, 1], -R[2, 0]))
+    else:
+        phi = math.degrees(math.atan2(R[1, 0], R[0, 0]))
+        psi = 0.0
+    return np.array([phi % 360.0, theta, psi % 360.0])
+
+
+def rotmat_zyz(euler_deg) -> np.ndarray:
+    phi, theta, psi = (math.radians(a) for a in euler_deg)
+
+    def rz(a):
+        return np.array([[math.cos(a), -math.sin(a), 0], [math.sin(a), math.cos(a), 0], [0, 0, 1]])
+
+    def ry(a):
+        return np.array([[math.cos(a), 0, math.sin(a)], [0, 1, 0], [-math.sin(a), 0, math.cos(a)]])
+
+    return rz(phi) @ ry(theta) @ rz(psi)
+
+
+def uniform_euler_grid(out_of_plane_step: float, in_plane_step: float) -> torch.Tensor:
+    """(N, 3) ZYZ Euler angles in degrees covering SO(3).
+
+    theta in [0, 180] every ``out_of_plane_step``; at each theta, phi spaced by
+    out_of_plane_step / sin(theta) over [0, 360); psi every ``in_plane_step``
+    over [0, 360).  ~ 4 pi / step^2 directions times 360 / psi_step rotations.
+    """
+    blocks = []
+    n_theta = int(round(180.0 / out_of_plane_step))
+    psis = np.arange(0.0, 360.0 - 1e-9, in_plane_step)
+    for it in range(n_theta + 1):
+        theta = min(180.0, it * out_of_plane_step)
+        n_phi = max(1, int(round(360.0 * math.sin(math.radians(theta)) / out_of_plane_step)))
+        phis = np.arange(n_phi) * (360.0 / n_phi)
+        ph, ps = np.meshgrid(phis, psis, indexing="ij")
+        blocks.append(np.stack([ph.ravel(), np.full(ph.size, theta), ps.ravel()], axis=1))
+    return torch.tensor(np.concatenate(blocks), dtype=torch.float32)
+
+
+def project_blobs(centres: np.ndarray, sigma: float, rot: np.ndarray, size: int, device="cpu") -> torch.Tensor:
+    """Exact line-integral projection (size x size, [y, x]) of the blob volume at rot."""
+    p = torch.tensor(centres @ rot, dtype=torch.float64, device=device)  # rows = (R^T c)^T
+    g = torch.arange(size, dtype=torch.float64, device=device) - size // 2
+    gx = torch.exp(-((g[None, :] - p[:, 0:1]) ** 2) / (2 * sigma**2))
+    gy = torch.exp(-((g[None, :] - p[:, 1:2]) ** 2) / (2 * sigma**2))
+    return (math.sqrt(2 * math.pi) * sigma * (gy.T @ gx)).to(torch.float32)
+
+
+@dataclass
+class MatchConfig:
+    image_shape: tuple[int, int] = (512, 512)
+    template_size: int = 64
+    n_blobs: int = 200
+    blob_sigma: float = 1.5
+    blob_radius: float = 24.0
+    pixel_size: float = 1.0
+    n_particles: int = 20
+    snr: float = 0.3
+    voltage: float = 300.0
+    spherical_aberration: float = 2.7
+    amplitude_contrast: float = 0.07
+    defocus: float = 12000.0
+    defocus_offsets: tuple[float, ...] = (0.0,)
+    pixel_size_offsets: tuple[float, ...] = (0.0,)
+    out_of_plane_step: float = 20.0
+    in_plane_step: float = 20.0
+    orientation_batch: int = 8
+    plant_from_grid: bool = True
+    seed: int = 0
+    name: str = "custom"
+
+
+# The two single-micrograph configurations of the plain method.
+CONFIG_SMALL = MatchConfig(name="2dtm-512sq-64cube-20deg")
+CONFIG_PRODUCTION = MatchConfig(
+    image_shape=(4096, 4096),
+    template_size=384,
+    n_blobs=4000,
+    blob_sigma=1.2,
+    blob_radius=150.0,
+    pixel_size=1.06,
+    n_particles=300,
+    snr=0.1,
+    defocus=10000.0,
+    defocus_offsets=(-200.0, 0.0, 200.0),
+    out_of_plane_step=2.5,
+    in_plane_step=1.5,
+    orientation_batch=8,
+    plant_from_grid=False,
+    name="2dtm-4096sq-384cube-2.5deg-1.5deg-3df",
+)
+
+
+@dataclass
+class MatchWorkload:
+    config: MatchConfig
+    kwargs: dict
+    planted: list = field(default_factory=list)  # (y0, x0, orientation index or -1, euler)
+    image: torch.Tensor | None = None
+
+
+def make_match_workload(cfg: MatchConfig, device="cpu", keep_image: bool = False,
+                        euler_angles: torch.Tensor | None = None) -> MatchWorkload:
+    """Build the ``core_match_template`` keyword arguments for ``cfg`` (CPU tensors)."""
+    H, W = cfg.image_shape
+    d = cfg.template_size
+    rng = np.random.default_rng(cfg.seed + 1)
+    vol, centres = blob_volume(d, cfg.n_blobs, cfg.blob_sigma, cfg.blob_radius, cfg.seed, device=device)
+    template_dft = pp.volume_to_rfft_fourier_slice(vol).cpu()
+    del vol
+    if euler_angles is None:
+        euler_angles = uniform_euler_grid(cfg.out_of_plane_step, cfg.in_plane_step)
+    gen = torch.Generator(device="cpu").manual_seed(cfg.seed + 2)
+    image = torch.randn((H, W), generator=gen, dtype=torch.float32).to(device)
+    box_ctf = pp.ctf_2d((d, d), cfg.defocus, 0.0, 0.0, cfg.voltage, cfg.spherical_aberration,
+                        cfg.amplitude_contrast, 0.0, cfg.pixel_size).to(device)
+    planted = []
+    for _ in range(cfg.n_particles):
+        if cfg.plant_from_grid:
+            oi = int(rng.integers(euler_angles.shape[0]))
+            eul = euler_angles[oi].double().numpy()
+        else:
+            oi = -1
+            q = rng.normal(size=4)
+            q /= np.linalg.norm(q)
+            w, x, y, z = q
+            Rq = np.array([
+                [1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)],
+            ])
+            eul = euler_zyz_from_rotmat(Rq)
+        proj = project_blobs(centres, cfg.blob_sigma, rotmat_zyz(eul), d, device=device)
+        proj = torch.fft.irfft2(torch.fft.rfft2(proj) * box_ctf, s=(d, d))
+        proj = proj - proj.mean()
+        proj = proj * (math.sqrt(cfg.snr) / proj.std().clamp_min(1e-12))
+        y0 = int(rng.integers(0, H - d + 1))
+        x0 = int(rng.integers(0, W - d + 1))
+        image[y0 : y0 + d, x0 : x0 + d] -= proj
+        planted.append((y0, x0, oi, tuple(float(a) for a in eul)))
+    image_dft = torch.fft.rfftn(image)
+    image_dft[0, 0] = 0 + 0j
+    wf_img = pp.whitening_filter(image_dft.cpu(), (H, W)).to(device)
+    wf_tmp = pp.whitening_filter(image_dft.cpu(), (d, d))
+    bandpass = torch.ones_like(wf_img)
+    image_dft = pp.preprocess_image(image_dft, wf_img, bandpass, (H, W), (H, W)).cpu()
+    defocus_offsets = torch.tensor(cfg.defocus_offsets, dtype=torch.float32)
+    pixel_offsets = torch.tensor(cfg.pixel_size_offsets, dtype=torch.float32)
+    ctf = pp.ctf_filter_stack(d, cfg.defocus, cfg.defocus, defocus_offsets, pixel_offsets,
+                              voltage=cfg.voltage, spherical_aberration=cfg.spherical_aberration,
+                              amplitude_contrast=cfg.amplitude_contrast, pixel_size=cfg.pixel_size)
+    kwargs = dict(
+        image_dft=image_dft.to(torch.complex64),
+        template_dft=template_dft.to(torch.complex64),
+        ctf_filters=ctf,
+        whitening_filter_template=wf_tmp,
+        defocus_values=defocus_offsets,
+        pixel_values=pixel_offsets,
+        euler_angles=euler_angles,
+    )
+    return MatchWorkload(cfg, kwargs, planted, image.cpu() if keep_image else None)
