@@ -278,7 +278,7 @@ def main():
     h2d = sum(v.numel() * v.element_size() for k, v in host.items() if k != "euler_angles") + chunk * 3 * 4
     e2e_times = []
     d2h = 0
-    for i in range(args.warmup + args.e2e_steps):
+    for i in range(args.warmup + args.e2e_steps if args.e2e_steps > 0 else 0):
         a, b = chunk_range(i)
         kw_i = dict(host)
         kw_i["euler_angles"] = host["euler_angles"][a:b]
@@ -289,7 +289,7 @@ def main():
         if i >= args.warmup:
             e2e_times.append(time.perf_counter() - t0)
         d2h = sum(v.numel() * v.element_size() for v in res.values() if isinstance(v, torch.Tensor))
-    e2e_val = chunk / statistics.median(e2e_times) * world
+    e2e_val = chunk / statistics.median(e2e_times) * world if e2e_times else None
 
     # --- CPU baseline (rank 0, N=1 only) ---------------------------------------
     cpu = None
