@@ -114,6 +114,27 @@ int lgb_match_search(const lgb_match_problem* problem, const void* template_dft,
                      int* best_index, double* corr_sum, double* corr_sq_sum, void* workspace,
                      size_t workspace_bytes, void* stream);
 
+/* lgb_match_search without any device allocation: no reference counterpart
+ * (the reference always allocates through PyTorch).  For callers that cannot
+ * call cudaMalloc -- code inside a host application that owns all device
+ * memory through its own pool, or that must avoid the implicit device
+ * synchronisation of cudaMalloc/cudaFree.  The caller passes every input and
+ * output (image_dft: device complex64 [H][W/2+1]; the rest as in
+ * lgb_match_search); scratch comes from a fixed array of
+ * lgb_static_scratch_capacity() bytes (32 MiB) compiled into the library and
+ * held by every GPU that loads it until the process exits.  Problems needing
+ * more scratch (see lgb_match_workspace_size) fail with
+ * LGB_ERR_WORKSPACE_TOO_SMALL.  The first call on a device resolves the
+ * array's device address (cudaGetSymbolAddress): make it before any stream
+ * capture.  All calls share the array and its contents persist between calls;
+ * calls whose GPU work overlaps race on it and must be serialised. */
+size_t lgb_static_scratch_capacity(void);
+int lgb_match_search_static_scratch(const lgb_match_problem* problem, const void* image_dft,
+                                    const void* template_dft, const float* projective_filters,
+                                    const float* euler_angles, int orientation_begin, int orientation_end,
+                                    float* mip, int* best_index, double* corr_sum, double* corr_sq_sum,
+                                    void* stream);
+
 /* Decode the best index and turn the sums into mean, standard deviation and
  * z-score (FP64 arithmetic, FP32 outputs; all maps device, H x W):
  *   corr_mean = S/total, corr_std = sqrt(max(S2/total - mean^2, 0)),

@@ -55,6 +55,8 @@ _SIGNATURES = {
     "lgb_match_prepare_image": ([_PROB, _P, _P, _SZ, _P], _I),
     "lgb_match_filters": ([_PROB, _P, _P, _P, _P], _I),
     "lgb_match_search": ([_PROB, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _SZ, _P], _I),
+    "lgb_static_scratch_capacity": ([], _SZ),
+    "lgb_match_search_static_scratch": ([_PROB, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P], _I),
     "lgb_match_finalize": ([_PROB, _LL, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
 }
 
