@@ -57,6 +57,7 @@ def _args():
     ap.add_argument("--cpu-sample-orient", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--config", choices=["production", "small"], default="production")
+    ap.add_argument("--batch", type=int, default=0, help="orientation batch (0: the configuration's)")
     return ap.parse_args()
 
 
@@ -208,7 +209,7 @@ def main():
     cfg = wl.config
     kw = wl.kwargs
     N = kw["euler_angles"].shape[0]
-    B = cfg.orientation_batch
+    B = args.batch or cfg.orientation_batch
     chunk = max(B, (args.orient_per_step // B) * B)
     search = MatchTemplateSearch(**kw, device=dev, orientation_batch_size=B)
     stream = torch.cuda.current_stream(dev)
