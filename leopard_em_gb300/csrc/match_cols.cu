@@ -1,5 +1,6 @@
 // Launcher: the fused column pass (forward FFT, cross power, inverse FFT) for
 // image height H.
+#include "match_fused.cuh"
 #include "match_kernels.cuh"
 #include "match_launch.h"
 
@@ -42,7 +43,45 @@ static int colpass_t(const void* A, const void* Ip, int h, int Wcp, int n_c, voi
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
+static int colpass_split(int groups, int n_c, int* per) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int split = 1;
+  while (split < n_c && groups * split < 4 * sms) split *= 2;
+  if (split > n_c) split = n_c;
+  *per = (n_c + split - 1) / split;
+  return (n_c + *per - 1) / *per;
+}
+
+template <int R, int P>
+static int colpass_fused_t(const void* A, const void* Ip, int h, int Wcp, int n_c, void* Y, cudaStream_t s) {
+  using CF = ColFused<R, P>;
+  if (cudaFuncSetAttribute(colpass_fused_kernel<R, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF::SMEM) !=
+      cudaSuccess)
+    return LGB_ERR_CUDA;
+  int per = 1;
+  const int groups = Wcp / kColGroup;
+  const int split = colpass_split(groups, n_c, &per);
+  dim3 grid(groups, split);
+  colpass_fused_kernel<R, P><<<grid, CF::THREADS, CF::SMEM, s>>>(
+      static_cast<const float2*>(A), static_cast<const float2*>(Ip), h, Wcp, n_c, per, static_cast<float2*>(Y));
+  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+}
+
 int launch_colpass(int H, const void* A, const void* Ip, int h, int Wcp, int n_c, void* Y, cudaStream_t s) {
+  switch (H) {
+    case 4096:
+      return colpass_fused_t<16, 3>(A, Ip, h, Wcp, n_c, Y, s);
+    case 512:
+      return colpass_fused_t<8, 3>(A, Ip, h, Wcp, n_c, Y, s);
+    case 256:
+      return colpass_fused_t<16, 2>(A, Ip, h, Wcp, n_c, Y, s);
+    case 64:
+      return colpass_fused_t<8, 2>(A, Ip, h, Wcp, n_c, Y, s);
+    default:
+      break;
+  }
   switch (H) {
 #define X(n) \
   case n:    \

@@ -1,0 +1,513 @@
+// Register-fused column and row passes of the plain FP32 search.
+//
+// colpass_fused_kernel<R, P>  (H = R^P, one butterfly per thread per pass)
+//   The forward FFT's last Stockham pass leaves element j + q*H/R of the
+//   column in thread j, and the inverse FFT's first pass consumes exactly those
+//   elements in the same thread: forward-last -> cross power -> inverse-first
+//   run in registers.  The pruned forward first pass reads its (at most two)
+//   non-zero inputs straight from global memory, the inverse last pass writes
+//   its outputs straight to global memory, so each correlogram column costs
+//   four shared-memory round trips instead of eight.  Twiddles come from a
+//   per-CTA shared table (built once with sincospif).  Thread layout: lane
+//   bits 0-1 select one of four adjacent columns, so each warp touches 8 rows
+//   x 32 B: whole sectors.
+//
+// rowpass_fused_kernel<WH, NT, Plan>  (W = 2*WH)
+//   The c2r pre-twiddle (X[k], conj X[WH-k] -> Z[k]) is applied while the
+//   first pass loads from the staged row; the last pass's outputs stay in
+//   registers and feed the statistics directly.  Rows are staged with
+//   cp.async double buffering (the next correlogram's row is in flight while
+//   the current one is transformed).  Waits are cp.async.wait_group: no spins.
+#pragma once
+
+#include <type_traits>
+
+#include "fft.cuh"
+#include "match_kernels.cuh"
+
+namespace lgb {
+
+// ---- radix-list helpers ----------------------------------------------------
+template <class RL>
+struct Head;
+template <int R, int... Rs>
+struct Head<Radices<R, Rs...>> {
+  static constexpr int value = R;
+};
+template <class RL>
+struct Last;
+template <int R>
+struct Last<Radices<R>> {
+  static constexpr int value = R;
+};
+template <int R, int R2, int... Rs>
+struct Last<Radices<R, R2, Rs...>> {
+  static constexpr int value = Last<Radices<R2, Rs...>>::value;
+};
+template <int R, class RL>
+struct Prepend;
+template <int R, int... Rs>
+struct Prepend<R, Radices<Rs...>> {
+  using type = Radices<R, Rs...>;
+};
+template <class RL>
+struct DropLast;
+template <int R>
+struct DropLast<Radices<R>> {
+  using type = Radices<>;
+};
+template <int R, int R2, int... Rs>
+struct DropLast<Radices<R, R2, Rs...>> {
+  using type = typename Prepend<R, typename DropLast<Radices<R2, Rs...>>::type>::type;
+};
+template <class RL>
+struct Tail;
+template <int R, int... Rs>
+struct Tail<Radices<R, Rs...>> {
+  using type = Radices<Rs...>;
+};
+// middle passes: drop first and last
+template <class RL>
+struct Middle {
+  using type = typename DropLast<typename Tail<RL>::type>::type;
+};
+
+// ---- async copy helpers (16-byte cp.async, completion via wait_group) -------
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// exp(-2 pi i r / 16), r = 0..15 (roots for the sparse first pass; R | 16)
+static __constant__ float2 kRootsFwd16[16] = {
+    {1.0f, 0.0f},
+    {0.92387953251128674f, -0.38268343236508977f},
+    {0.70710678118654752f, -0.70710678118654752f},
+    {0.38268343236508977f, -0.92387953251128674f},
+    {0.0f, -1.0f},
+    {-0.38268343236508977f, -0.92387953251128674f},
+    {-0.70710678118654752f, -0.70710678118654752f},
+    {-0.92387953251128674f, -0.38268343236508977f},
+    {-1.0f, 0.0f},
+    {-0.92387953251128674f, 0.38268343236508977f},
+    {-0.70710678118654752f, 0.70710678118654752f},
+    {-0.38268343236508977f, 0.92387953251128674f},
+    {0.0f, 1.0f},
+    {0.38268343236508977f, 0.92387953251128674f},
+    {0.70710678118654752f, 0.70710678118654752f},
+    {0.92387953251128674f, 0.38268343236508977f},
+};
+
+// Padded shared-memory access at base + q*STEP.  With IdxPad16 and STEP a
+// multiple of 16, f(base + q*STEP) = f(base) + q*(STEP + STEP/16): one index
+// computation and compile-time offsets for the whole butterfly.
+template <class IDX, int STEP>
+__device__ __forceinline__ int padded_at(int fbase, int base, int q) {
+  if constexpr (std::is_same<IDX, IdxPad16>::value && STEP % 16 == 0) {
+    return fbase + q * (STEP + STEP / 16);
+  } else {
+    return IDX::f(base + q * STEP);
+  }
+}
+// f(R*j + q) for q < R <= 16 and R | 16: R*j + (R*j >> 4) + q.
+template <int R>
+__device__ __forceinline__ int padded_first(int j) {
+  static_assert(16 % R == 0, "radix must divide 16");
+  return R * j + ((R * j) >> 4);
+}
+
+// Value of v that the compiler cannot treat as loop invariant: keeps per-row
+// address arithmetic inside the loop instead of holding 16 hoisted addresses.
+__device__ __forceinline__ int opaque(int v) {
+  int r;
+  asm volatile("mov.b32 %0, %1;" : "=r"(r) : "r"(v));
+  return r;
+}
+
+// ---- twiddles from a shared table ------------------------------------------
+// table row for k: w^t = exp(-2 pi i k t / L), t = 1..R-1 (forward sign);
+// the inverse uses the conjugates.
+template <int R, int DIR>
+__device__ __forceinline__ void twiddle_from_table(float2* v, const float2* row) {
+#pragma unroll
+  for (int t = 1; t < R; ++t) {
+    const float2 w = row[t - 1];
+    v[t] = DIR < 0 ? cmul(v[t], w) : cmulc(v[t], w);
+  }
+}
+
+// Fill the twiddle table of one Stockham pass (NS, R): NS rows of R-1 entries.
+template <int NS, int R>
+__device__ __forceinline__ void fill_twiddles(float2* tab, int tid, int nthreads) {
+  constexpr int L = NS * R;
+  for (int e = tid; e < NS * (R - 1); e += nthreads) {
+    const int k = e / (R - 1), t = e % (R - 1) + 1;
+    float s, c;
+    sincospif(2.0f * (float)((k * t) % L) / (float)L, &s, &c);
+    tab[e] = make_float2(c, -s);
+  }
+}
+
+// Shared-memory Stockham pass with table twiddles (in place, two barriers).
+template <int N, int R, int NS, int NT, int DIR, class IDX>
+__device__ __forceinline__ void table_pass(float2* __restrict__ x, const float2* __restrict__ tab, int t) {
+  constexpr int NB = N / R;
+  constexpr int PER = (NB + NT - 1) / NT;
+  float2 v[PER][R];
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int j = t + p * NT;
+    if ((NB % NT == 0) || j < NB) {
+      const int fj = IDX::f(j);
+#pragma unroll
+      for (int q = 0; q < R; ++q) v[p][q] = x[padded_at<IDX, NB>(fj, j, q)];
+      if (NS > 1) twiddle_from_table<R, DIR>(v[p], tab + (j % NS) * (R - 1));
+      Dft<R, DIR>::run(v[p]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int j = t + p * NT;
+    if ((NB % NT == 0) || j < NB) {
+      const int base = (j / NS) * NS * R + (j % NS);
+      const int fb = IDX::f(base);
+#pragma unroll
+      for (int q = 0; q < R; ++q) x[padded_at<IDX, NS>(fb, base, q)] = v[p][q];
+    }
+  }
+  __syncthreads();
+}
+
+// Table offsets: pass with stride NS starts at sum over earlier passes of NS'*(R'-1).
+template <int NS, class RL>
+struct TableSize;
+template <int NS>
+struct TableSize<NS, Radices<>> {
+  static constexpr int value = 0;
+};
+template <int NS, int R, int... Rs>
+struct TableSize<NS, Radices<R, Rs...>> {
+  static constexpr int value = (NS > 1 ? NS * (R - 1) : 0) + TableSize<NS * R, Radices<Rs...>>::value;
+};
+
+template <int N, int NS, class RL>
+struct FillTables;
+template <int N, int NS>
+struct FillTables<N, NS, Radices<>> {
+  static __device__ __forceinline__ void run(float2*, int, int) {}
+};
+template <int N, int NS, int R, int... Rs>
+struct FillTables<N, NS, Radices<R, Rs...>> {
+  static __device__ __forceinline__ void run(float2* tab, int tid, int nt) {
+    if (NS > 1) fill_twiddles<NS, R>(tab, tid, nt);
+    FillTables<N, NS * R, Radices<Rs...>>::run(tab + (NS > 1 ? NS * (R - 1) : 0), tid, nt);
+  }
+};
+
+// Run a list of middle passes (shared memory in place), starting at stride NS,
+// with twiddles from `tab` (laid out by TableSize/FillTables from stride NS0).
+template <int N, int NT, int DIR, class IDX, int NS, class RL>
+struct TablePasses;
+template <int N, int NT, int DIR, class IDX, int NS>
+struct TablePasses<N, NT, DIR, IDX, NS, Radices<>> {
+  static __device__ __forceinline__ void run(float2*, const float2*, int) {}
+};
+template <int N, int NT, int DIR, class IDX, int NS, int R, int... Rs>
+struct TablePasses<N, NT, DIR, IDX, NS, Radices<R, Rs...>> {
+  static __device__ __forceinline__ void run(float2* x, const float2* tab, int t) {
+    table_pass<N, R, NS, NT, DIR, IDX>(x, tab, t);
+    TablePasses<N, NT, DIR, IDX, NS * R, Radices<Rs...>>::run(x, tab + (NS > 1 ? NS * (R - 1) : 0), t);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Fused column pass for H = R^P.
+// ---------------------------------------------------------------------------
+template <int R, int P>
+struct UniformPlan;
+template <int R>
+struct UniformPlan<R, 2> {
+  using type = Radices<R, R>;
+  static constexpr int N = R * R;
+};
+template <int R>
+struct UniformPlan<R, 3> {
+  using type = Radices<R, R, R>;
+  static constexpr int N = R * R * R;
+};
+
+template <int R, int P>
+struct ColFused {
+  using RL = typename UniformPlan<R, P>::type;
+  static constexpr int N = UniformPlan<R, P>::N;
+  static constexpr int NB = N / R;                    // butterflies per pass = threads per column
+  static constexpr int THREADS = kColGroup * NB;
+  static constexpr int STRIDE = IdxPad16::pad(N) + 4; // column stride in shared memory (float2)
+  static constexpr int TAB = TableSize<1, RL>::value; // twiddle entries of passes 2..P
+  static constexpr size_t SMEM = sizeof(float2) * (size_t)(kColGroup * STRIDE + TAB);
+};
+
+template <int R, int P>
+__global__ void __launch_bounds__(ColFused<R, P>::THREADS, 1)
+    colpass_fused_kernel(const float2* __restrict__ A, const float2* __restrict__ Ip, int h, int Wcp, int n_c,
+                         int c_per_block, float2* __restrict__ Y) {
+  using CF = ColFused<R, P>;
+  using RL = typename CF::RL;
+  constexpr int N = CF::N, NB = CF::NB, STRIDE = CF::STRIDE;
+  constexpr int NS_LAST = N / R;
+  extern __shared__ float2 csm[];
+  float2* tab = csm + kColGroup * STRIDE;
+  FillTables<N, 1, RL>::run(tab, threadIdx.x, CF::THREADS);
+  // twiddle sub-table of the last pass (stride NS_LAST)
+  const float2* tab_last = tab + TableSize<1, typename DropLast<RL>::type>::value;
+  const float2* tab_mid = tab;  // middle passes start at stride R (first pass has none)
+
+  const int lane = threadIdx.x & 31;
+  const int g = lane & 3;                             // column within the group
+  const int j = (threadIdx.x >> 5) * 8 + (lane >> 2); // butterfly index
+  float2* x = csm + g * STRIDE;
+  const int kx = blockIdx.x * kColGroup + g;
+  const int c_begin = blockIdx.y * c_per_block;
+  const int c_end = min(n_c, c_begin + c_per_block);
+  // first-pass sparse form: at most two non-zero inputs per butterfly when h <= 2*NB
+  const bool sparse = h <= 2 * NB;
+  __syncthreads();
+
+  const int fj = IdxPad16::f(j);
+  const int f1 = padded_first<R>(j);
+#pragma unroll 1
+  for (int c = c_begin; c < c_end; ++c) {
+    float2 v[R];
+    const size_t ws = (size_t)opaque(Wcp);  // row stride, re-derived per correlogram
+    const float2* a = A + (size_t)c * h * ws + kx;
+    // ---- forward pass 1 (stride 1, inputs from global, rows >= h are zero)
+    if (sparse) {
+      const float2 x0 = j < h ? __ldg(a + (size_t)j * ws) : make_float2(0.f, 0.f);
+      const float2 x1 = j + NB < h ? __ldg(a + (size_t)(j + NB) * ws) : make_float2(0.f, 0.f);
+      // y[r] = x0 + x1 * exp(-2 pi i r / R)
+      static_assert(16 % R == 0, "sparse first pass needs R | 16");
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[r] = cadd(x0, cmul(x1, kRootsFwd16[r * (16 / R)]));
+    } else {
+      const float2* ar = a + (size_t)j * ws;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        v[q] = j + q * NB < h ? __ldg(ar) : make_float2(0.f, 0.f);
+        ar += NB * ws;
+      }
+      Dft<R, -1>::run(v);
+    }
+#pragma unroll
+    for (int q = 0; q < R; ++q) x[f1 + q] = v[q];
+    __syncthreads();
+    // ---- forward middle passes
+    TablePasses<N, NB, -1, IdxPad16, R, typename Middle<RL>::type>::run(x, tab_mid, j);
+    // ---- forward last pass -> registers
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[q] = x[padded_at<IdxPad16, NB>(fj, j, q)];
+    twiddle_from_table<R, -1>(v, tab_last + j * (R - 1));
+    Dft<R, -1>::run(v);
+    // v[q] = P[row j + q*NB]; cross power with the image spectrum, P[0,0] = 0
+    {
+      const float2* ip = Ip + (size_t)j * ws + kx;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        const float2 I = __ldg(ip);
+        ip += NB * ws;
+        v[q] = (q == 0 && j == 0 && kx == 0) ? make_float2(0.f, 0.f) : cmulc(I, v[q]);
+      }
+    }
+    // ---- inverse pass 1 in registers (stride 1, no twiddles)
+    Dft<R, +1>::run(v);
+    __syncthreads();  // everyone has read the forward last pass inputs
+#pragma unroll
+    for (int q = 0; q < R; ++q) x[f1 + q] = v[q];
+    __syncthreads();
+    TablePasses<N, NB, +1, IdxPad16, R, typename Middle<RL>::type>::run(x, tab_mid, j);
+    // ---- inverse last pass -> global
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[q] = x[padded_at<IdxPad16, NB>(fj, j, q)];
+    twiddle_from_table<R, +1>(v, tab_last + j * (R - 1));
+    Dft<R, +1>::run(v);
+    float2* yo = Y + (size_t)c * N * ws + (size_t)j * ws + kx;
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      *yo = v[q];
+      yo += NB * ws;
+    }
+    __syncthreads();  // before the next correlogram's first-pass stores
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Fused row pass (c2r of length 2*WH + statistics).
+// ---------------------------------------------------------------------------
+template <int WH, int NT, class RL>
+struct RowFused {
+  static constexpr int R1 = Head<RL>::value;
+  static constexpr int RLAST = Last<RL>::value;
+  static constexpr int NB1 = WH / R1;
+  static constexpr int PER1 = (NB1 + NT - 1) / NT;
+  static constexpr int NBL = WH / RLAST;
+  static constexpr int PERL = NBL / NT;
+  static constexpr int ZS = IdxPad16::pad(WH) + 2;
+  static constexpr int TAB = TableSize<1, RL>::value;
+  static_assert(NBL % NT == 0, "last pass must give every thread whole butterflies");
+  static_assert(NB1 <= NT * PER1, "first pass coverage");
+  static size_t smem(int wcp) { return sizeof(float2) * (size_t)(2 * wcp + ZS + TAB + WH); }
+};
+
+template <int WH, int NT, class RL>
+__global__ void __launch_bounds__(NT, 2)
+    rowpass_fused_kernel(const float2* __restrict__ Y, int H, int Wcp, int n_c, int nb, int n_orient, int o0,
+                         float scale, float* __restrict__ mip, int* __restrict__ best, double* __restrict__ s1,
+                         double* __restrict__ s2) {
+  using RF = RowFused<WH, NT, RL>;
+  constexpr int R1 = RF::R1, RLAST = RF::RLAST, NB1 = RF::NB1, PER1 = RF::PER1, NBL = RF::NBL, PERL = RF::PERL;
+  constexpr int OUT = PERL * RLAST;  // complex outputs (pixel pairs) per thread
+  extern __shared__ float2 rsm[];
+  float2* xr0 = rsm;
+  float2* xr1 = rsm + Wcp;
+  float2* z = rsm + 2 * Wcp;
+  float2* tab = z + RF::ZS;
+  float2* pre = tab + RF::TAB;  // c2r pre-twiddle exp(+i pi k / WH)
+  const int y = blockIdx.x;
+  const int t = threadIdx.x;
+  const int n16 = Wcp / 2;  // 16-byte chunks per row
+
+  // stage row 0 while the tables are built
+  {
+    const float2* src = Y + (size_t)y * Wcp;
+    for (int i = t; i < n16; i += NT) cp_async16(xr0 + 2 * i, src + 2 * i);
+    cp_async_commit();
+  }
+  FillTables<WH, 1, RL>::run(tab, t, NT);
+  for (int k = t; k < WH; k += NT) {
+    float s, c;
+    sincospif((float)k / (float)WH, &s, &c);
+    pre[k] = make_float2(c, s);
+  }
+  const float2* tab_last = tab + TableSize<1, typename DropLast<RL>::type>::value;
+
+  float bmax[2 * OUT], bs[2 * OUT], bss[2 * OUT];
+  int barg[2 * OUT];
+#pragma unroll
+  for (int i = 0; i < 2 * OUT; ++i) {
+    bmax[i] = -INFINITY;
+    barg[i] = 0;
+    bs[i] = 0.f;
+    bss[i] = 0.f;
+  }
+
+#pragma unroll 1
+  for (int c = 0; c < n_c; ++c) {
+    const float2* xr = (c & 1) ? xr1 : xr0;
+    if (c + 1 < n_c) {
+      float2* nxt = (c & 1) ? xr0 : xr1;
+      const float2* src = Y + ((size_t)(c + 1) * H + y) * Wcp;
+      for (int i = t; i < n16; i += NT) cp_async16(nxt + 2 * i, src + 2 * i);
+      cp_async_commit();
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    // ---- pass 1: pre-twiddle while loading, no twiddles (stride 1)
+    {
+      float2 v[PER1][R1];
+#pragma unroll
+      for (int p = 0; p < PER1; ++p) {
+        const int j = t + p * NT;
+        if ((NB1 % NT == 0) || j < NB1) {
+#pragma unroll
+          for (int q = 0; q < R1; ++q) {
+            const int k = j + q * NB1;
+            float2 a = xr[k];
+            float2 b = xr[WH - k];
+            if (k == 0) {
+              a.y = 0.f;
+              b.y = 0.f;
+            }
+            b.y = -b.y;
+            const float2 xo = cmul(csub(a, b), pre[k]);
+            v[p][q] = cadd(cadd(a, b), mul_i<1>(xo));
+          }
+          Dft<R1, +1>::run(v[p]);
+        }
+      }
+#pragma unroll
+      for (int p = 0; p < PER1; ++p) {
+        const int j = t + p * NT;
+        if ((NB1 % NT == 0) || j < NB1) {
+#pragma unroll
+          for (int q = 0; q < R1; ++q) z[IdxPad16::f(j * R1 + q)] = v[p][q];
+        }
+      }
+    }
+    __syncthreads();
+    TablePasses<WH, NT, +1, IdxPad16, R1, typename Middle<RL>::type>::run(z, tab, t);
+    // ---- last pass -> registers -> statistics
+#pragma unroll
+    for (int p = 0; p < PERL; ++p) {
+      const int j = t + p * NT;
+      float2 v[RLAST];
+#pragma unroll
+      for (int q = 0; q < RLAST; ++q) v[q] = z[IdxPad16::f(j + q * NBL)];
+      twiddle_from_table<RLAST, +1>(v, tab_last + j * (RLAST - 1));
+      Dft<RLAST, +1>::run(v);
+#pragma unroll
+      for (int q = 0; q < RLAST; ++q) {
+        const int o = 2 * (p * RLAST + q);
+        const float a = v[q].x * scale, b = v[q].y * scale;
+        if (a > bmax[o]) { bmax[o] = a; barg[o] = c; }
+        if (b > bmax[o + 1]) { bmax[o + 1] = b; barg[o + 1] = c; }
+        bs[o] += a;
+        bss[o] = fmaf(a, a, bss[o]);
+        bs[o + 1] += b;
+        bss[o + 1] = fmaf(b, b, bss[o + 1]);
+      }
+    }
+    __syncthreads();
+  }
+
+  const size_t W = 2 * (size_t)WH;
+#pragma unroll
+  for (int p = 0; p < PERL; ++p) {
+#pragma unroll
+    for (int q = 0; q < RLAST; ++q) {
+      const int o = 2 * (p * RLAST + q);
+      const int m = t + p * NT + q * NBL;
+      const size_t idx = (size_t)y * W + 2 * (size_t)m;
+      float2 mm = *reinterpret_cast<float2*>(mip + idx);
+      int2 bi = *reinterpret_cast<int2*>(best + idx);
+      double2 sa = *reinterpret_cast<double2*>(s1 + idx);
+      double2 sq = *reinterpret_cast<double2*>(s2 + idx);
+      if (bmax[o] > mm.x) {
+        mm.x = bmax[o];
+        const int cc = barg[o];
+        bi.x = (cc / nb) * n_orient + o0 + (cc - (cc / nb) * nb);
+      }
+      if (bmax[o + 1] > mm.y) {
+        mm.y = bmax[o + 1];
+        const int cc = barg[o + 1];
+        bi.y = (cc / nb) * n_orient + o0 + (cc - (cc / nb) * nb);
+      }
+      sa.x += (double)bs[o];
+      sa.y += (double)bs[o + 1];
+      sq.x += (double)bss[o];
+      sq.y += (double)bss[o + 1];
+      *reinterpret_cast<float2*>(mip + idx) = mm;
+      *reinterpret_cast<int2*>(best + idx) = bi;
+      *reinterpret_cast<double2*>(s1 + idx) = sa;
+      *reinterpret_cast<double2*>(s2 + idx) = sq;
+    }
+  }
+}
+
+}  // namespace lgb

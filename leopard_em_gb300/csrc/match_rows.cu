@@ -1,5 +1,6 @@
 // Launchers: zero-padded projection rfft and the row c2r + statistics pass
 // (image width W).
+#include "match_fused.cuh"
 #include "match_kernels.cuh"
 #include "match_launch.h"
 
@@ -54,9 +55,33 @@ int launch_pad_rfft(int W, const float* proj, const double* rowstats, int h, int
   }
 }
 
+template <int WH, int NT, class RL>
+static int rowpass_fused_t(const void* Y, int H, int Wcp, int n_c, int nb, int n_orient, int o0, float* mip,
+                           int* best, double* s1, double* s2, cudaStream_t s) {
+  using RF = RowFused<WH, NT, RL>;
+  const size_t smem = RF::smem(Wcp);
+  if (cudaFuncSetAttribute(rowpass_fused_kernel<WH, NT, RL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return LGB_ERR_CUDA;
+  const float scale = 1.0f / ((float)H * (float)(2 * WH));
+  rowpass_fused_kernel<WH, NT, RL><<<H, NT, smem, s>>>(static_cast<const float2*>(Y), H, Wcp, n_c, nb, n_orient, o0,
+                                                       scale, mip, best, s1, s2);
+  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+}
+
 int launch_rowpass(int W, const void* Y, int H, int Wcp, int n_c, int nb, int n_orient, int o0, float* mip,
                    int* best, double* s1, double* s2, cudaStream_t s) {
   if (W % 2) return LGB_ERR_UNSUPPORTED_SIZE;
+  switch (W / 2) {
+    case 2048:
+      return rowpass_fused_t<2048, 256, Radices<8, 8, 8, 4>>(Y, H, Wcp, n_c, nb, n_orient, o0, mip, best, s1, s2, s);
+    case 1024:
+      return rowpass_fused_t<1024, 256, Radices<8, 8, 4, 4>>(Y, H, Wcp, n_c, nb, n_orient, o0, mip, best, s1, s2, s);
+    case 256:
+      return rowpass_fused_t<256, 64, Radices<8, 8, 4>>(Y, H, Wcp, n_c, nb, n_orient, o0, mip, best, s1, s2, s);
+    default:
+      break;
+  }
   switch (W / 2) {
 #define X(n) \
   case n:    \

@@ -110,6 +110,8 @@ def _small_workload(H, W, d, n_o, n_df=1, n_cs=1, seed=3):
         (256, 512, 48, 12, 2, 1, 3),
         (288, 288, 64, 10, 3, 2, 5),
         (512, 512, 64, 16, 1, 1, 8),
+        (4096, 4096, 64, 4, 2, 1, 4),   # production FFT lengths (fused column/row kernels)
+        (4096, 4096, 384, 2, 1, 1, 2),  # production template size
     ],
 )
 def test_against_oracle_fp64_statistics(H, W, d, n_o, n_df, n_cs, batch):
