@@ -83,6 +83,10 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// L2 placement: measured, neither an evict_last policy on the image-spectrum
+// loads nor streaming stores of the intermediate help -- both take L2 away
+// from the correlogram rows that the row pass re-reads right after.
+
 // exp(-2 pi i r / 16), r = 0..15 (roots for the sparse first pass; R | 16)
 static __constant__ float2 kRootsFwd16[16] = {
     {1.0f, 0.0f},
@@ -132,21 +136,24 @@ __device__ __forceinline__ int opaque(int v) {
 // ---- twiddles from a shared table ------------------------------------------
 // table row for k: w^t = exp(-2 pi i k t / L), t = 1..R-1 (forward sign);
 // the inverse uses the conjugates.
-template <int R, int DIR>
-__device__ __forceinline__ void twiddle_from_table(float2* v, const float2* row) {
+// Table of one Stockham pass (stride NS, radix R): entry (t, k) =
+// exp(-2 pi i k t / (NS R)) at tab[(t-1)*NS + k], t = 1..R-1, k < NS.  Lanes
+// reading consecutive k hit consecutive addresses (no bank conflicts); lanes
+// sharing k broadcast.  The inverse uses the conjugates.
+template <int R, int DIR, int NS>
+__device__ __forceinline__ void twiddle_from_table(float2* v, const float2* tab, int k) {
 #pragma unroll
   for (int t = 1; t < R; ++t) {
-    const float2 w = row[t - 1];
+    const float2 w = tab[(t - 1) * NS + k];
     v[t] = DIR < 0 ? cmul(v[t], w) : cmulc(v[t], w);
   }
 }
 
-// Fill the twiddle table of one Stockham pass (NS, R): NS rows of R-1 entries.
 template <int NS, int R>
 __device__ __forceinline__ void fill_twiddles(float2* tab, int tid, int nthreads) {
   constexpr int L = NS * R;
   for (int e = tid; e < NS * (R - 1); e += nthreads) {
-    const int k = e / (R - 1), t = e % (R - 1) + 1;
+    const int t = e / NS + 1, k = e % NS;
     float s, c;
     sincospif(2.0f * (float)((k * t) % L) / (float)L, &s, &c);
     tab[e] = make_float2(c, -s);
@@ -166,7 +173,7 @@ __device__ __forceinline__ void table_pass(float2* __restrict__ x, const float2*
       const int fj = IDX::f(j);
 #pragma unroll
       for (int q = 0; q < R; ++q) v[p][q] = x[padded_at<IDX, NB>(fj, j, q)];
-      if (NS > 1) twiddle_from_table<R, DIR>(v[p], tab + (j % NS) * (R - 1));
+      if (NS > 1) twiddle_from_table<R, DIR, NS>(v[p], tab, j % NS);
       Dft<R, DIR>::run(v[p]);
     }
   }
@@ -281,6 +288,14 @@ __global__ void __launch_bounds__(ColFused<R, P>::THREADS, 1)
 
   const int fj = IdxPad16::f(j);
   const int f1 = padded_first<R>(j);
+  // sparse inputs of the first correlogram; later ones are prefetched one
+  // correlogram ahead, while the current one runs its middle passes
+  float2 nx0 = make_float2(0.f, 0.f), nx1 = make_float2(0.f, 0.f);
+  if (sparse && c_begin < c_end) {
+    const float2* a = A + (size_t)c_begin * h * Wcp + kx;
+    if (j < h) nx0 = __ldg(a + (size_t)j * Wcp);
+    if (j + NB < h) nx1 = __ldg(a + (size_t)(j + NB) * Wcp);
+  }
 #pragma unroll 1
   for (int c = c_begin; c < c_end; ++c) {
     float2 v[R];
@@ -288,8 +303,12 @@ __global__ void __launch_bounds__(ColFused<R, P>::THREADS, 1)
     const float2* a = A + (size_t)c * h * ws + kx;
     // ---- forward pass 1 (stride 1, inputs from global, rows >= h are zero)
     if (sparse) {
-      const float2 x0 = j < h ? __ldg(a + (size_t)j * ws) : make_float2(0.f, 0.f);
-      const float2 x1 = j + NB < h ? __ldg(a + (size_t)(j + NB) * ws) : make_float2(0.f, 0.f);
+      const float2 x0 = nx0, x1 = nx1;
+      if (c + 1 < c_end) {
+        const float2* an = a + (size_t)h * ws;
+        nx0 = j < h ? __ldg(an + (size_t)j * ws) : make_float2(0.f, 0.f);
+        nx1 = j + NB < h ? __ldg(an + (size_t)(j + NB) * ws) : make_float2(0.f, 0.f);
+      }
       // y[r] = x0 + x1 * exp(-2 pi i r / R)
       static_assert(16 % R == 0, "sparse first pass needs R | 16");
 #pragma unroll
@@ -311,7 +330,7 @@ __global__ void __launch_bounds__(ColFused<R, P>::THREADS, 1)
     // ---- forward last pass -> registers
 #pragma unroll
     for (int q = 0; q < R; ++q) v[q] = x[padded_at<IdxPad16, NB>(fj, j, q)];
-    twiddle_from_table<R, -1>(v, tab_last + j * (R - 1));
+    twiddle_from_table<R, -1, NS_LAST>(v, tab_last, j);
     Dft<R, -1>::run(v);
     // v[q] = P[row j + q*NB]; cross power with the image spectrum, P[0,0] = 0
     {
@@ -333,7 +352,7 @@ __global__ void __launch_bounds__(ColFused<R, P>::THREADS, 1)
     // ---- inverse last pass -> global
 #pragma unroll
     for (int q = 0; q < R; ++q) v[q] = x[padded_at<IdxPad16, NB>(fj, j, q)];
-    twiddle_from_table<R, +1>(v, tab_last + j * (R - 1));
+    twiddle_from_table<R, +1, NS_LAST>(v, tab_last, j);
     Dft<R, +1>::run(v);
     float2* yo = Y + (size_t)c * N * ws + (size_t)j * ws + kx;
 #pragma unroll
@@ -459,7 +478,7 @@ __global__ void __launch_bounds__(NT, 2)
       float2 v[RLAST];
 #pragma unroll
       for (int q = 0; q < RLAST; ++q) v[q] = z[IdxPad16::f(j + q * NBL)];
-      twiddle_from_table<RLAST, +1>(v, tab_last + j * (RLAST - 1));
+      twiddle_from_table<RLAST, +1, NBL>(v, tab_last, j);
       Dft<RLAST, +1>::run(v);
 #pragma unroll
       for (int q = 0; q < RLAST; ++q) {
