@@ -146,6 +146,60 @@ int lgb_match_finalize(const lgb_match_problem* problem, long long total_positio
                        float* best_phi, float* best_theta, float* best_psi, float* best_defocus,
                        float* corr_mean, float* corr_std, void* stream);
 
+/* ------------------------------------------------------------------------ */
+/* Local-grid refinement (core_refine_template.py:33-202, :555-767)          */
+/* ------------------------------------------------------------------------ */
+
+/* Shape of one refinement call: P particle crops of H x W against a cubic
+ * template of edge d, over K Euler-angle offsets (in batches of B), D defocus
+ * offsets and C pixel-size offsets.  The valid crop is (H-d+1) x (W-d+1). */
+typedef struct lgb_refine_problem {
+  int image_h;
+  int image_w;
+  int template_size;
+  int n_pixel_sizes;
+  int n_defocus;
+  int n_offsets;
+  int offset_batch;
+  int n_particles;
+} lgb_refine_problem;
+
+/* Microscope parameters of the CTF (ctf_utils.py:19-116 ctf_kwargs). */
+typedef struct lgb_ctf_params {
+  double voltage_kv;
+  double spherical_aberration_mm;
+  double amplitude_contrast;
+  double b_factor;          /* B envelope exp(-B k^2 / 4), A^2 */
+  double phase_shift_deg;
+  double pixel_size;        /* A; the CTF grid and the Cs <-> pixel-size relation */
+} lgb_ctf_params;
+
+/* 1 if every FFT length of this refinement is compiled in, else 0. */
+int lgb_refine_supported(const lgb_refine_problem* problem);
+
+/* Bytes of device scratch lgb_refine_search needs. */
+int lgb_refine_workspace_size(const lgb_refine_problem* problem, size_t* bytes);
+
+/* Replaces _core_refine_template_single_thread (core_refine_template.py:555-767)
+ * for P particles at once.  Device inputs: particle_stack_dft complex64
+ * [P][H][W/2+1]; template_dft complex64 [d][d][d/2+1] (fftshifted); euler_angles
+ * [P][3] and euler_offsets [K][3] (ZYZ degrees); defocus_u/v/angle [P] (A, A,
+ * degrees); defocus_offsets [D] (A); pixel_size_offsets [C] (A); corr_mean /
+ * corr_std [P][H-d+1][W-d+1]; projective_filters [P][d][d/2+1].  Per particle
+ * the CTF stack (C x D, from `ctf`) times the projective filter filters each
+ * slice; rotations are R(offset) @ R(particle).  Outputs (device, [P]): best
+ * z-score and the largest correlation of the batch that produced it, the
+ * winning flat index f = (y*(W-d+1) + x)*C*D*n + c (c = (cs*D + df)*n + b within
+ * that batch of n offsets starting at best_offset_begin), or -1 if no batch
+ * beat the initial -1e9. */
+int lgb_refine_search(const lgb_refine_problem* problem, const lgb_ctf_params* ctf, const void* particle_stack_dft,
+                      const void* template_dft, const float* euler_angles, const float* euler_offsets,
+                      const float* defocus_u, const float* defocus_v, const float* defocus_angle,
+                      const float* defocus_offsets, const float* pixel_size_offsets, const float* corr_mean,
+                      const float* corr_std, const float* projective_filters, float* best_z, float* best_cc,
+                      int* best_flat, int* best_offset_begin, int* best_batch_len, void* workspace,
+                      size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

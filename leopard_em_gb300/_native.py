@@ -38,6 +38,34 @@ class MatchProblem(ctypes.Structure):
     ]
 
 
+class RefineProblem(ctypes.Structure):
+    """Mirror of ``lgb_refine_problem``."""
+
+    _fields_ = [
+        ("image_h", ctypes.c_int),
+        ("image_w", ctypes.c_int),
+        ("template_size", ctypes.c_int),
+        ("n_pixel_sizes", ctypes.c_int),
+        ("n_defocus", ctypes.c_int),
+        ("n_offsets", ctypes.c_int),
+        ("offset_batch", ctypes.c_int),
+        ("n_particles", ctypes.c_int),
+    ]
+
+
+class CtfParams(ctypes.Structure):
+    """Mirror of ``lgb_ctf_params``."""
+
+    _fields_ = [
+        ("voltage_kv", ctypes.c_double),
+        ("spherical_aberration_mm", ctypes.c_double),
+        ("amplitude_contrast", ctypes.c_double),
+        ("b_factor", ctypes.c_double),
+        ("phase_shift_deg", ctypes.c_double),
+        ("pixel_size", ctypes.c_double),
+    ]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _LL = ctypes.c_longlong
@@ -57,6 +85,9 @@ _SIGNATURES = {
     "lgb_match_search": ([_PROB, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _SZ, _P], _I),
     "lgb_static_scratch_capacity": ([], _SZ),
     "lgb_match_search_static_scratch": ([_PROB, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P], _I),
+    "lgb_refine_supported": ([ctypes.POINTER(RefineProblem)], _I),
+    "lgb_refine_workspace_size": ([ctypes.POINTER(RefineProblem), ctypes.POINTER(_SZ)], _I),
+    "lgb_refine_search": ([ctypes.POINTER(RefineProblem), ctypes.POINTER(CtfParams)] + [_P] * 18 + [_SZ, _P], _I),
     "lgb_match_finalize": ([_PROB, _LL, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
 }
 

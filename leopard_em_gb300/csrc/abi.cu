@@ -267,11 +267,11 @@ int lgb_match_search(const lgb_match_problem* p, const void* template_dft, const
     const int n_c = n_cd * nb;
     {
       StageScope sc(LGB_STAGE_SLICE, s);
-      if ((st = launch_slice(template_dft, h, euler_angles, o0, nb, slices, s))) return st;
+      if ((st = launch_slice(template_dft, h, euler_angles, o0, nb, nullptr, slices, s))) return st;
     }
     {
       StageScope sc(LGB_STAGE_PROJ_COL, s);
-      if ((st = launch_proj_col(h, slices, projective_filters, nb, n_c, T, s))) return st;
+      if ((st = launch_proj_col(h, slices, projective_filters, nb, n_cd, n_c, T, s))) return st;
     }
     {
       StageScope sc(LGB_STAGE_PROJ_ROW, s);
@@ -283,7 +283,7 @@ int lgb_match_search(const lgb_match_problem* p, const void* template_dft, const
     }
     {
       StageScope sc(LGB_STAGE_COLPASS, s);
-      if ((st = launch_colpass(H, A, ip, h, L.wcp, n_c, Y, s))) return st;
+      if ((st = launch_colpass(H, A, ip, h, L.wcp, n_c, n_c, H, Y, s))) return st;
     }
     {
       StageScope sc(LGB_STAGE_ROWPASS, s);

@@ -20,7 +20,8 @@ bool supported_col(int H) {
 }
 
 template <int HN>
-static int colpass_t(const void* A, const void* Ip, int h, int Wcp, int n_c, void* Y, cudaStream_t s) {
+static int colpass_t(const void* A, const void* Ip, int h, int Wcp, int n_c, int cpi, int y_rows, void* Y,
+                     cudaStream_t s) {
   constexpr int NT = FftThreads<HN>::value;
   const size_t smem = sizeof(float2) * kColGroup * (IdxPad16::pad(HN) + 4);
   if (cudaFuncSetAttribute(colpass_kernel<HN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
@@ -38,8 +39,8 @@ static int colpass_t(const void* A, const void* Ip, int h, int Wcp, int n_c, voi
   split = (n_c + per - 1) / per;
   dim3 grid(groups, split);
   colpass_kernel<HN><<<grid, kColGroup * NT, smem, s>>>(static_cast<const float2*>(A),
-                                                       static_cast<const float2*>(Ip), h, Wcp, n_c, per,
-                                                       static_cast<float2*>(Y));
+                                                       static_cast<const float2*>(Ip), h, Wcp, n_c, per, cpi,
+                                                       y_rows, static_cast<float2*>(Y));
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
@@ -55,7 +56,8 @@ static int colpass_split(int groups, int n_c, int* per) {
 }
 
 template <int R, int P>
-static int colpass_fused_t(const void* A, const void* Ip, int h, int Wcp, int n_c, void* Y, cudaStream_t s) {
+static int colpass_fused_t(const void* A, const void* Ip, int h, int Wcp, int n_c, int cpi, int y_rows, void* Y,
+                           cudaStream_t s) {
   using CF = ColFused<R, P>;
   if (cudaFuncSetAttribute(colpass_fused_kernel<R, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF::SMEM) !=
       cudaSuccess)
@@ -65,27 +67,30 @@ static int colpass_fused_t(const void* A, const void* Ip, int h, int Wcp, int n_
   const int split = colpass_split(groups, n_c, &per);
   dim3 grid(groups, split);
   colpass_fused_kernel<R, P><<<grid, CF::THREADS, CF::SMEM, s>>>(
-      static_cast<const float2*>(A), static_cast<const float2*>(Ip), h, Wcp, n_c, per, static_cast<float2*>(Y));
+      static_cast<const float2*>(A), static_cast<const float2*>(Ip), h, Wcp, n_c, per, cpi, y_rows,
+      static_cast<float2*>(Y));
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
-int launch_colpass(int H, const void* A, const void* Ip, int h, int Wcp, int n_c, void* Y, cudaStream_t s) {
+int launch_colpass(int H, const void* A, const void* Ip, int h, int Wcp, int n_c, int cpi, int y_rows, void* Y,
+                   cudaStream_t s) {
+  if (cpi < 1 || y_rows < 1 || y_rows > H) return LGB_ERR_INVALID_ARGUMENT;
   switch (H) {
     case 4096:
-      return colpass_fused_t<16, 3>(A, Ip, h, Wcp, n_c, Y, s);
+      return colpass_fused_t<16, 3>(A, Ip, h, Wcp, n_c, cpi, y_rows, Y, s);
     case 512:
-      return colpass_fused_t<8, 3>(A, Ip, h, Wcp, n_c, Y, s);
+      return colpass_fused_t<8, 3>(A, Ip, h, Wcp, n_c, cpi, y_rows, Y, s);
     case 256:
-      return colpass_fused_t<16, 2>(A, Ip, h, Wcp, n_c, Y, s);
+      return colpass_fused_t<16, 2>(A, Ip, h, Wcp, n_c, cpi, y_rows, Y, s);
     case 64:
-      return colpass_fused_t<8, 2>(A, Ip, h, Wcp, n_c, Y, s);
+      return colpass_fused_t<8, 2>(A, Ip, h, Wcp, n_c, cpi, y_rows, Y, s);
     default:
       break;
   }
   switch (H) {
 #define X(n) \
   case n:    \
-    return colpass_t<n>(A, Ip, h, Wcp, n_c, Y, s);
+    return colpass_t<n>(A, Ip, h, Wcp, n_c, cpi, y_rows, Y, s);
     LGB_COL_SIZES(X)
 #undef X
     default:

@@ -263,7 +263,7 @@ struct ColFused {
 template <int R, int P>
 __global__ void __launch_bounds__(ColFused<R, P>::THREADS, 1)
     colpass_fused_kernel(const float2* __restrict__ A, const float2* __restrict__ Ip, int h, int Wcp, int n_c,
-                         int c_per_block, float2* __restrict__ Y) {
+                         int c_per_block, int c_per_image, int y_rows, float2* __restrict__ Y) {
   using CF = ColFused<R, P>;
   using RL = typename CF::RL;
   constexpr int N = CF::N, NB = CF::NB, STRIDE = CF::STRIDE;
@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(ColFused<R, P>::THREADS, 1)
     Dft<R, -1>::run(v);
     // v[q] = P[row j + q*NB]; cross power with the image spectrum, P[0,0] = 0
     {
-      const float2* ip = Ip + (size_t)j * ws + kx;
+      const float2* ip = Ip + (size_t)(c / c_per_image) * N * ws + (size_t)j * ws + kx;
 #pragma unroll
       for (int q = 0; q < R; ++q) {
         const float2 I = __ldg(ip);
@@ -354,10 +354,10 @@ __global__ void __launch_bounds__(ColFused<R, P>::THREADS, 1)
     for (int q = 0; q < R; ++q) v[q] = x[padded_at<IdxPad16, NB>(fj, j, q)];
     twiddle_from_table<R, +1, NS_LAST>(v, tab_last, j);
     Dft<R, +1>::run(v);
-    float2* yo = Y + (size_t)c * N * ws + (size_t)j * ws + kx;
+    float2* yo = Y + (size_t)c * y_rows * ws + (size_t)j * ws + kx;
 #pragma unroll
     for (int q = 0; q < R; ++q) {
-      *yo = v[q];
+      if (j + q * NB < y_rows) *yo = v[q];
       yo += NB * ws;
     }
     __syncthreads();  // before the next correlogram's first-pass stores

@@ -50,17 +50,19 @@ __device__ inline void euler_zyz_to_rotmat(const float* e, float* R) {
 // ---------------------------------------------------------------------------
 template <int HT, int COLS>
 __global__ void __launch_bounds__(COLS* FftThreads<HT>::value)
-    proj_col_kernel(const float2* __restrict__ slices, const float* __restrict__ pf, int nb,
+    proj_col_kernel(const float2* __restrict__ slices, const float* __restrict__ pf, int nb, int n_cd,
                     float2* __restrict__ T) {
   constexpr int NT = FftThreads<HT>::value;
   constexpr int WC = HT / 2 + 1;
   constexpr int STRIDE = IdxPad16::pad(HT) + 2;
   __shared__ float2 buf[COLS * STRIDE];
+  // c = (p*n_cd + cd)*nb + b: slices are per (p, b), filters per (p, cd)
   const int c = blockIdx.y;
-  const int cd = c / nb, b = c - (c / nb) * nb;
+  const int pc = c / nb, b = c - (c / nb) * nb;
+  const int p = pc / n_cd;
+  const float2* sl = slices + ((size_t)p * nb + b) * HT * WC;
+  const float* f = pf + (size_t)pc * HT * WC;
   const int kx0 = blockIdx.x * COLS;
-  const float2* sl = slices + (size_t)b * HT * WC;
-  const float* f = pf + (size_t)cd * HT * WC;
   for (int e = threadIdx.x; e < HT * COLS; e += blockDim.x) {
     const int y = e / COLS, i = e % COLS, kx = kx0 + i;
     float2 v = make_float2(0.f, 0.f);
@@ -158,6 +160,7 @@ __global__ void __launch_bounds__(ROWS* FftThreads<HT / 2>::value)
 
 // Normalisation constants of utils.py:106-188 from the per-row moments:
 // returns edge mean e and scale s such that normalised = (p - e) * s.
+// Called by all 32 lanes of warp 0 (the launcher guarantees a full warp).
 __device__ inline void projection_norm_constants(const double* rs, int h, int H, int W, float* e_out,
                                                  float* s_out) {
   // warp 0 reduces h rows
@@ -243,7 +246,7 @@ __global__ void __launch_bounds__(ROWS* FftThreads<WH>::value)
 template <int HN>
 __global__ void __launch_bounds__(kColGroup* FftThreads<HN>::value, 1)
     colpass_kernel(const float2* __restrict__ A, const float2* __restrict__ Ip, int h, int Wcp, int n_c,
-                   int c_per_block, float2* __restrict__ Y) {
+                   int c_per_block, int c_per_image, int y_rows, float2* __restrict__ Y) {
   constexpr int NT = FftThreads<HN>::value;
   constexpr int STRIDE = IdxPad16::pad(HN) + 4;
   extern __shared__ float2 cbuf[];
@@ -263,9 +266,10 @@ __global__ void __launch_bounds__(kColGroup* FftThreads<HN>::value, 1)
     __syncthreads();
     block_fft_pruned_outline<HN, NT, -1, IdxPad16>(cbuf + g * STRIDE, t, h);
 #pragma unroll 2
+    const float2* ipc = Ip + (size_t)(c / c_per_image) * HN * Wcp;
     for (int e = threadIdx.x; e < HN * kColGroup; e += NTH) {
       const int y = e / kColGroup, i = e % kColGroup;
-      const float2 I = __ldg(Ip + (size_t)y * Wcp + kx0 + i);
+      const float2 I = __ldg(ipc + (size_t)y * Wcp + kx0 + i);
       const int si = i * STRIDE + IdxPad16::f(y);
       float2 X = cmulc(I, cbuf[si]);
       if (y == 0 && kx0 + i == 0) X = make_float2(0.f, 0.f);
@@ -273,9 +277,9 @@ __global__ void __launch_bounds__(kColGroup* FftThreads<HN>::value, 1)
     }
     __syncthreads();
     block_fft_outline<HN, NT, +1, IdxPad16>(cbuf + g * STRIDE, t);
-    float2* yo = Y + (size_t)c * HN * Wcp + kx0;
+    float2* yo = Y + (size_t)c * y_rows * Wcp + kx0;
 #pragma unroll 2
-    for (int e = threadIdx.x; e < HN * kColGroup; e += NTH) {
+    for (int e = threadIdx.x; e < y_rows * kColGroup; e += NTH) {
       const int y = e / kColGroup, i = e % kColGroup;
       yo[(size_t)y * Wcp + i] = cbuf[i * STRIDE + IdxPad16::f(y)];
     }

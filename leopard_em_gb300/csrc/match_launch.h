@@ -9,12 +9,24 @@ namespace lgb {
 
 // Each returns an lgb_status; LGB_ERR_UNSUPPORTED_SIZE when the FFT length is
 // not instantiated.
-int launch_slice(const void* vol, int d, const float* euler, int o0, int nb, void* slices, cudaStream_t s);
-int launch_proj_col(int h, const void* slices, const float* pf, int nb, int n_c, void* T, cudaStream_t s);
+// Slices for nb rotations: from Euler angles euler[o0 + b] (rotations == nullptr)
+// or from row-major 3x3 matrices rotations[9*b].
+int launch_slice(const void* vol, int d, const float* euler, int o0, int nb, const float* rotations, void* slices,
+                 cudaStream_t s);
+// Refine row pass (valid crop, z-score, per-particle packed arg-max); see refine.cu.
+int launch_refine_rowpass(int W, const void* Y, int y_rows, int Wcp, int n_cpp, int n_particles, int crop_h,
+                          int crop_w, float scale, const float* corr_mean, const float* corr_std,
+                          unsigned long long* slot_key, unsigned* slot_cc, cudaStream_t s);
+bool supported_refine_row(int W);
+// c = (p*n_cd + cd)*nb + b; slices [P][nb], filters [P][n_cd] (P = n_c / (n_cd*nb))
+int launch_proj_col(int h, const void* slices, const float* pf, int nb, int n_cd, int n_c, void* T, cudaStream_t s);
 int launch_proj_row(int h, const void* T, int n_c, float* proj, double* rowstats, cudaStream_t s);
 int launch_pad_rfft(int W, const float* proj, const double* rowstats, int h, int H, int Wcp, int n_c, void* A,
                     cudaStream_t s);
-int launch_colpass(int H, const void* A, const void* Ip, int h, int Wcp, int n_c, void* Y, cudaStream_t s);
+// Ip holds one padded spectrum per image; correlogram c uses image c / c_per_image.
+// Only rows y < y_rows of each inverse column transform are stored (Y is [n_c][y_rows][Wcp]).
+int launch_colpass(int H, const void* A, const void* Ip, int h, int Wcp, int n_c, int c_per_image, int y_rows,
+                   void* Y, cudaStream_t s);
 int launch_rowpass(int W, const void* Y, int H, int Wcp, int n_c, int nb, int n_orient, int o0, float* mip,
                    int* best, double* s1, double* s2, cudaStream_t s);
 

@@ -10,10 +10,16 @@ namespace lgb {
 // fftshifted slice), DC set to 0, multiplied by -1.
 // ---------------------------------------------------------------------------
 __global__ void slice_kernel(const float2* __restrict__ vol, int d, const float* __restrict__ euler, int o0,
-                             float2* __restrict__ slices) {
+                             const float* __restrict__ rotations, float2* __restrict__ slices) {
   const int b = blockIdx.y;
   __shared__ float R[9];
-  if (threadIdx.x == 0) euler_zyz_to_rotmat(euler + 3 * (size_t)(o0 + b), R);
+  if (threadIdx.x == 0) {
+    if (rotations) {
+      for (int i = 0; i < 9; ++i) R[i] = rotations[9 * (size_t)b + i];
+    } else {
+      euler_zyz_to_rotmat(euler + 3 * (size_t)(o0 + b), R);
+    }
+  }
   __syncthreads();
   const int wc = d / 2 + 1;
   const int n_el = d * wc;
@@ -69,10 +75,12 @@ bool supported_template(int h) {
   }
 }
 
-int launch_slice(const void* vol, int d, const float* euler, int o0, int nb, void* slices, cudaStream_t s) {
+int launch_slice(const void* vol, int d, const float* euler, int o0, int nb, const float* rotations, void* slices,
+                 cudaStream_t s) {
   const int n_el = d * (d / 2 + 1);
   dim3 grid((n_el + 255) / 256, nb);
-  slice_kernel<<<grid, 256, 0, s>>>(static_cast<const float2*>(vol), d, euler, o0, static_cast<float2*>(slices));
+  slice_kernel<<<grid, 256, 0, s>>>(static_cast<const float2*>(vol), d, euler, o0, rotations,
+                                    static_cast<float2*>(slices));
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
@@ -80,11 +88,11 @@ constexpr int kProjCols = 8;
 constexpr int kProjRows = 8;
 
 template <int HT>
-static int proj_col_t(const void* slices, const float* pf, int nb, int n_c, void* T, cudaStream_t s) {
+static int proj_col_t(const void* slices, const float* pf, int nb, int n_cd, int n_c, void* T, cudaStream_t s) {
   constexpr int WC = HT / 2 + 1;
   dim3 grid((WC + kProjCols - 1) / kProjCols, n_c);
   proj_col_kernel<HT, kProjCols><<<grid, kProjCols * FftThreads<HT>::value, 0, s>>>(
-      static_cast<const float2*>(slices), pf, nb, static_cast<float2*>(T));
+      static_cast<const float2*>(slices), pf, nb, n_cd, static_cast<float2*>(T));
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
@@ -97,11 +105,11 @@ static int proj_row_t(const void* T, int n_c, float* proj, double* rowstats, cud
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
-int launch_proj_col(int h, const void* slices, const float* pf, int nb, int n_c, void* T, cudaStream_t s) {
+int launch_proj_col(int h, const void* slices, const float* pf, int nb, int n_cd, int n_c, void* T, cudaStream_t s) {
   switch (h) {
 #define X(n) \
   case n:    \
-    return proj_col_t<n>(slices, pf, nb, n_c, T, s);
+    return proj_col_t<n>(slices, pf, nb, n_cd, n_c, T, s);
     LGB_TEMPLATE_SIZES(X)
 #undef X
     default:

@@ -7,7 +7,7 @@
 namespace lgb {
 
 // W/2 values
-#define LGB_ROW_SIZES(X) X(32) X(40) X(64) X(128) X(144) X(256) X(288) X(512) X(1024) X(2048)
+#define LGB_ROW_SIZES(X) X(24) X(32) X(40) X(64) X(128) X(144) X(256) X(288) X(512) X(1024) X(2048)
 
 bool supported_row(int W) {
   if (W % 2) return false;
@@ -25,7 +25,10 @@ template <int WH>
 static int pad_rfft_t(const float* proj, const double* rowstats, int h, int H, int Wcp, int n_c, void* A,
                       cudaStream_t s) {
   constexpr int NT = FftThreads<WH>::value;
-  constexpr int ROWS = NT >= 128 ? 2 : (NT >= 32 ? 4 : 8);
+  // at least one full warp: the normalisation reduction shuffles across warp 0
+  constexpr int ROWS0 = NT >= 128 ? 2 : (NT >= 32 ? 4 : 8);
+  constexpr int ROWS = ROWS0 * NT >= 32 ? ROWS0 : (32 + NT - 1) / NT;
+  static_assert(ROWS * NT >= 32, "pad_rfft CTA must hold a full warp");
   dim3 grid((h + ROWS - 1) / ROWS, n_c);
   pad_rfft_kernel<WH, ROWS><<<grid, ROWS * NT, 0, s>>>(proj, rowstats, h, H, Wcp, static_cast<float2*>(A));
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;

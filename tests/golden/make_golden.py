@@ -18,8 +18,17 @@ and is therefore restated in this script's ``_run_search``).
 
 Outputs ``tests/golden/match_small.npz``: inputs and outputs of two small
 searches (one with several defocus planes and pixel sizes, run with the
-reference's batched CPU path and per-batch statistics update).  The files are
-small (< 1 MB) and committed; this script is not needed at test time.
+reference's batched CPU path and per-batch statistics update).
+
+``tests/golden/refine_small.npz``: per-particle results of the reference's
+``_core_refine_template_single_thread`` (backend/core_refine_template.py:555-767,
+its CPU branch), with roma / torch_fourier_slice / torch_ctf /
+torch_fourier_filter replaced by the oracle's restatements
+(``oracle/ref_refine_template.py``) and the rest -- ctf_utils.py,
+search_utils.py, the cross-correlation, z-score, strict-'>' batch update and
+index decode -- the reference's own code.
+
+The files are small and committed; this script is not needed at test time.
 """
 
 from __future__ import annotations
@@ -37,6 +46,7 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
 from oracle import ref_match_template as orc  # noqa: E402
+from oracle import ref_refine_template as orr  # noqa: E402
 
 
 def _install_stubs():
@@ -48,7 +58,28 @@ def _install_stubs():
 
     roma.euler_to_rotmat = euler_to_rotmat
     roma.rotmat_composition = lambda seq: seq[0] @ seq[1]
+    roma.rotmat_to_euler = lambda convention, R, degrees=True, **_: orr.rotmat_to_euler_zyz(R).to(R.dtype)
     sys.modules["roma"] = roma
+
+    tctf = types.ModuleType("torch_ctf")
+
+    def calculate_ctf_2d(defocus, astigmatism, astigmatism_angle, voltage, spherical_aberration, amplitude_contrast,
+                         phase_shift, pixel_size, image_shape, rfft=True, fftshift=False, even_zernike_coeffs=None,
+                         odd_zernike_coeffs=None, transform_matrix=None):
+        assert rfft and not fftshift and even_zernike_coeffs is None and odd_zernike_coeffs is None
+        assert transform_matrix is None
+        return orr.calculate_ctf_2d(defocus, astigmatism, astigmatism_angle, voltage, float(spherical_aberration),
+                                    amplitude_contrast, phase_shift, pixel_size, tuple(image_shape))
+
+    tctf.calculate_ctf_2d = calculate_ctf_2d
+    sys.modules["torch_ctf"] = tctf
+    tff = types.ModuleType("torch_fourier_filter")
+    env = types.ModuleType("torch_fourier_filter.envelopes")
+    env.b_envelope = lambda B, image_shape, pixel_size, rfft=True, fftshift=False, device=None: orr.b_envelope(
+        B, tuple(image_shape), pixel_size)
+    tff.envelopes = env
+    sys.modules["torch_fourier_filter"] = tff
+    sys.modules["torch_fourier_filter.envelopes"] = env
 
     tfs = types.ModuleType("torch_fourier_slice")
     tfs.extract_central_slices_rfft_3d = (
@@ -181,6 +212,76 @@ def main(ref_root):
     out["decode/defocus"] = dfv.numpy()
     out["decode/out"] = torch.stack([phi, theta, psi, dd]).numpy()
     path = os.path.join(HERE, "match_small.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+    _refine_golden(ref_root)
+
+
+def _refine_golden(ref_root):
+    for name in ("leopard_em.utils",):
+        sys.modules.setdefault(name, types.ModuleType(name))
+    su = _load(ref_root, "utils/search_utils.py", "leopard_em.utils.search_utils")
+    _load(ref_root, "utils/cross_correlation.py", "leopard_em.utils.cross_correlation")
+    _load(ref_root, "utils/ctf_utils.py", "leopard_em.utils.ctf_utils")
+    _load(ref_root, "backend/distributed.py", "leopard_em.backend.distributed")
+    sys.modules["leopard_em.backend.cross_correlation"] = sys.modules["leopard_em_ref_cc"]
+    rt = _load(ref_root, "backend/core_refine_template.py", "leopard_em_ref_refine")
+    assert su.get_cs_range is not None
+    g = torch.Generator().manual_seed(31)
+    n_p, H, d = 3, 48, 32
+    wc = d // 2 + 1
+    inp = _make_inputs(31, H, H, d, 1, 1, 1)
+    template_dft = inp["template_dft"]
+    stack = []
+    for _ in range(n_p):
+        im = torch.randn(H, H, generator=g)
+        f = torch.fft.rfftn(im)
+        f[0, 0] = 0
+        f = f / torch.sqrt((f.abs() ** 2).sum() * 2) * (H * H) ** 0.5
+        stack.append(f)
+    particle_stack_dft = torch.stack(stack).to(torch.complex64)
+    euler = (torch.rand(n_p, 3, generator=g) * torch.tensor([360.0, 180.0, 360.0])).to(torch.float32)
+    offsets = torch.tensor([[0.0, 0.0, 0.0], [2.0, 0.0, -2.0], [-2.0, 1.5, 0.0], [0.0, -1.5, 2.0],
+                            [1.0, 1.0, 1.0], [-1.0, -1.0, 3.0]], dtype=torch.float32)
+    defocus_offsets = torch.tensor([-100.0, 0.0, 100.0])
+    pixel_offsets = torch.tensor([-0.01, 0.01])
+    du = torch.tensor([9000.0, 10000.0, 11000.0])
+    dv = du - 150.0
+    dang = torch.tensor([10.0, 35.0, 80.0])
+    crop = H - d + 1
+    corr_mean = 0.05 * torch.randn(n_p, crop, crop, generator=g)
+    corr_std = 0.8 + 0.4 * torch.rand(n_p, crop, crop, generator=g)
+    pf = (1.0 / (1.0 + 2.0 * torch.fft.rfftfreq(d)[None, :] ** 2 + torch.fft.fftfreq(d)[:, None] ** 2)).expand(
+        n_p, d, wc).contiguous().to(torch.float32)
+    ctf_kwargs = dict(voltage=300.0, spherical_aberration=2.7, amplitude_contrast_ratio=0.07, ctf_B_factor=60.0,
+                      phase_shift=0.0, pixel_size=1.0, template_shape=(d, d), even_zernikes=None,
+                      odd_zernikes=None, mag_matrix=None)
+    keys = ["max_cc", "max_z_score", "refined_phi_offset", "refined_theta_offset", "refined_psi_offset",
+            "refined_defocus_offset", "refined_pixel_size_offset", "refined_pos_y", "refined_pos_x", "angle_idx"]
+    res = {k: [] for k in keys}
+    for i in range(n_p):
+        st = rt._core_refine_template_single_thread(
+            particle_image_dft=particle_stack_dft[i], particle_index=i, template_dft=template_dft,
+            euler_angles=euler[i], euler_angle_offsets=offsets, defocus_u=float(du[i]), defocus_v=float(dv[i]),
+            defocus_angle=float(dang[i]), defocus_offsets=defocus_offsets, pixel_size_offsets=pixel_offsets,
+            corr_mean=corr_mean[i], corr_std=corr_std[i], ctf_kwargs=ctf_kwargs, projective_filter=pf[i],
+            batch_size=4)
+        for k in keys:
+            res[k].append(float(st[k]))
+    out = {
+        "in/particle_stack_dft": particle_stack_dft.numpy(), "in/template_dft": template_dft.numpy(),
+        "in/euler_angles": euler.numpy(), "in/euler_angle_offsets": offsets.numpy(),
+        "in/defocus_offsets": defocus_offsets.numpy(), "in/pixel_size_offsets": pixel_offsets.numpy(),
+        "in/defocus_u": du.numpy(), "in/defocus_v": dv.numpy(), "in/defocus_angle": dang.numpy(),
+        "in/corr_mean": corr_mean.numpy(), "in/corr_std": corr_std.numpy(), "in/projective_filters": pf.numpy(),
+        "in/batch_size": np.array(4),
+    }
+    for k, v in ctf_kwargs.items():
+        if k != "template_shape" and v is not None:
+            out[f"ctf/{k}"] = np.array(v)
+    for k in keys:
+        out[f"out/{k}"] = np.array(res[k])
+    path = os.path.join(HERE, "refine_small.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, os.path.getsize(path), "bytes")
 

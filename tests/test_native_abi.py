@@ -61,3 +61,13 @@ def test_status_maps_to_python_exceptions(lib):
     with pytest.raises(RuntimeError):
         _native.check(_native.LGB_ERR_CUDA, "x")
     _native.check(_native.LGB_OK, "x")
+
+
+def test_ctypes_signatures_match_header_arity(lib):
+    """Every binding in _native has exactly the parameter count the header declares."""
+    src = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "leopard_gb300.h")).read(), flags=re.S)
+    for m in re.finditer(r"\b(lgb_\w+)\s*\(([^;]*?)\);", src, flags=re.S):
+        name, params = m.group(1), m.group(2).strip()
+        n = 0 if params in ("void", "") else len(params.split(","))
+        assert name in _native._SIGNATURES, name
+        assert len(_native._SIGNATURES[name][0]) == n, name

@@ -86,3 +86,45 @@ def test_projection_slice_theorem_fixes_rotation_convention():
     err_good = np.abs(proj - good).max() / np.abs(good).max()
     err_bad = np.abs(proj - bad).max() / np.abs(bad).max()
     assert err_good < 0.2 and err_bad > 3 * err_good
+
+
+# ---------------------------------------------------------------------------
+# refinement (core_refine_template.py:555-767) against the reference's own code
+# ---------------------------------------------------------------------------
+from oracle import ref_refine_template as orr  # noqa: E402
+
+RGOLD = np.load(os.path.join(os.path.dirname(__file__), "golden", "refine_small.npz"))
+
+
+def refine_golden_inputs():
+    keys = ["particle_stack_dft", "template_dft", "euler_angles", "euler_angle_offsets", "defocus_offsets",
+            "pixel_size_offsets", "defocus_u", "defocus_v", "defocus_angle", "corr_mean", "corr_std",
+            "projective_filters"]
+    kw = {k: torch.from_numpy(RGOLD[f"in/{k}"]) for k in keys}
+    ctf = {k.split("/", 1)[1]: RGOLD[k].item() for k in RGOLD.files if k.startswith("ctf/")}
+    ctf.update(template_shape=(kw["template_dft"].shape[1], kw["template_dft"].shape[1]), even_zernikes=None,
+               odd_zernikes=None, mag_matrix=None)
+    kw["ctf_kwargs"] = ctf
+    return kw, int(RGOLD["in/batch_size"])
+
+
+def test_refine_single_particle_matches_reference():
+    kw, b = refine_golden_inputs()
+    for i in range(kw["particle_stack_dft"].shape[0]):
+        st = orr.refine_single_particle(
+            kw["particle_stack_dft"][i], kw["template_dft"], kw["euler_angles"][i], kw["euler_angle_offsets"],
+            kw["defocus_u"][i], kw["defocus_v"][i], kw["defocus_angle"][i], kw["defocus_offsets"],
+            kw["pixel_size_offsets"], kw["corr_mean"][i], kw["corr_std"][i], kw["ctf_kwargs"],
+            kw["projective_filters"][i], b)
+        for k in ["max_cc", "max_z_score"]:
+            assert abs(st[k] - RGOLD[f"out/{k}"][i]) <= 1e-4 * abs(RGOLD[f"out/{k}"][i])
+        for k in ["refined_phi_offset", "refined_theta_offset", "refined_psi_offset", "refined_defocus_offset",
+                  "refined_pixel_size_offset", "refined_pos_y", "refined_pos_x", "angle_idx"]:
+            assert st[k] == RGOLD[f"out/{k}"][i], k
+
+
+def test_rotmat_euler_round_trip():
+    e = torch.tensor([[10.0, 40.0, 300.0], [200.0, 120.0, 15.0], [359.0, 179.0, 1.0]], dtype=torch.float64)
+    back = orr.rotmat_to_euler_zyz(orc.euler_to_rotmat_zyz(e, dtype=torch.float64))
+    back = torch.where(back < 0, back + 360, back)
+    assert torch.allclose(back, e, atol=1e-9)
