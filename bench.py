@@ -58,6 +58,8 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--config", choices=["production", "small"], default="production")
     ap.add_argument("--batch", type=int, default=0, help="orientation batch (0: the configuration's)")
+    ap.add_argument("--refine-particles", type=int, default=4)
+    ap.add_argument("--no-refine", action="store_true")
     return ap.parse_args()
 
 
@@ -157,6 +159,56 @@ def _peaks():
             return json.load(f), "measured"
     except Exception:
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def refine_bench(args, dev, with_cpu):
+    """Refined particles/s of the plain local grid (288^2 crops, 256^3 template,
+    +-3 deg @ 0.25 deg x +-400 A @ 50 A)."""
+    from leopard_em_gb300 import synthetic as sy
+    from leopard_em_gb300.backend import core_refine_template
+    from leopard_em_gb300.backend.core_refine_template import refine_particles_device
+
+    cfg = sy.CONFIG_REFINE
+    n = args.refine_particles
+    kw, _ = sy.make_refine_workload(cfg, n, device=dev)
+    dkw = {k: (v.to(dev) if isinstance(v, torch.Tensor) else v) for k, v in kw.items()}
+    warm = dict(dkw)
+    warm["euler_angle_offsets"] = dkw["euler_angle_offsets"][: 2 * cfg.batch]
+    refine_particles_device(**warm, device=dev, batch_size=cfg.batch)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    raw = refine_particles_device(**dkw, device=dev, batch_size=cfg.batch)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    dev_s = e0.elapsed_time(e1) / 1e3
+    t0 = time.perf_counter()
+    res = core_refine_template(**kw, device=dev, batch_size=cfg.batch)
+    e2e_s = time.perf_counter() - t0
+    K = int(kw["euler_angle_offsets"].shape[0])
+    D = int(kw["defocus_offsets"].shape[0])
+    out = {
+        "metric": "refined particles/s (plain local grid)", "value": n / dev_s, "unit": "particles/s",
+        "e2e": n / e2e_s, "particles": n, "offsets": K, "defocus": D,
+        "cross_correlations_per_particle": K * D, "cross_correlations_per_s": n * K * D / dev_s,
+        "mean_refined_snr": float(res["refined_z_score"].mean()),
+        "workload": cfg.name,
+    }
+    if with_cpu:
+        from oracle import ref_refine_template as orr
+
+        m = 16
+        ck = {k: v for k, v in kw.items()}
+        ck["euler_angle_offsets"] = kw["euler_angle_offsets"][:m]
+        sub = {k: (v[:1] if isinstance(v, torch.Tensor) and v.shape[0] == n else v) for k, v in ck.items()}
+        torch.set_num_threads(os.cpu_count() or 1)
+        t0 = time.perf_counter()
+        orr.core_refine_template_cpu(**sub, batch_size=m)
+        cpu_s = (time.perf_counter() - t0) * K / m
+        out["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": "particles/s", "cores": os.cpu_count() or 1,
+                               "kind": "port", "sample": f"1 particle x {m} offsets x {D} defocus, extrapolated to {K} offsets"}
+    return out
 
 
 def run_reference(args):
@@ -303,6 +355,10 @@ def main():
                "sample": f"{n} orientations x {n_cd} defocus of the {cfg.name} workload, CPU oracle "
                          "(torch.fft/pocketfft restatement of the reference's CPU path)"}
 
+    refine = None
+    if rank == 0 and world == 1 and not args.no_refine:
+        refine = refine_bench(args, dev, with_cpu=not args.no_cpu_baseline)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -316,6 +372,7 @@ def main():
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": gpu_launches,
             "clocks": clocks.summary(),
+            "refine": refine,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -217,3 +217,120 @@ def make_match_workload(cfg: MatchConfig, device="cpu", keep_image: bool = False
         euler_angles=euler_angles,
     )
     return MatchWorkload(cfg, kwargs, planted, image.cpu() if keep_image else None)
+
+
+def local_euler_offsets(out_of_plane_range: float, out_of_plane_step: float, in_plane_range: float,
+                        in_plane_step: float) -> torch.Tensor:
+    """(K, 3) ZYZ offsets around the identity for local refinement.
+
+    Tilt directions on rings theta = 0, step, 2*step, ... <= range, each ring
+    with round(2*pi*sin(theta)/step) azimuths phi (a pure tilt is
+    (phi, theta, -phi)), combined with in-plane offsets psi in
+    [-in_plane_range, in_plane_range] every in_plane_step.
+    """
+    rows = []
+    n_t = int(math.floor(out_of_plane_range / out_of_plane_step + 1e-9))
+    psis = np.arange(-in_plane_range, in_plane_range + 1e-9, in_plane_step)
+    for it in range(n_t + 1):
+        theta = it * out_of_plane_step
+        n_phi = 1 if it == 0 else max(1, int(round(2 * math.pi * math.sin(math.radians(theta))
+                                                    / math.radians(out_of_plane_step))))
+        for ip in range(n_phi):
+            phi = ip * 360.0 / n_phi
+            for psi in psis:
+                rows.append((phi, theta, -phi + psi))
+    return torch.tensor(rows, dtype=torch.float32)
+
+
+@dataclass
+class RefineConfig:
+    crop: int = 288
+    template_size: int = 256
+    n_blobs: int = 4000
+    blob_sigma: float = 1.2
+    blob_radius: float = 100.0
+    pixel_size: float = 1.06
+    snr_range: tuple[float, float] = (0.05, 0.2)
+    shift_px: float = 3.0
+    defocus: float = 10000.0
+    defocus_jitter: float = 400.0
+    pose_perturbation_deg: float = 3.0
+    grid_angle_range: float = 3.0
+    grid_angle_step: float = 0.25
+    grid_defocus_range: float = 400.0
+    grid_defocus_step: float = 50.0
+    batch: int = 32
+    seed: int = 0
+    name: str = "refine-288sq-256cube-3deg@0.25-400A@50"
+
+
+CONFIG_REFINE = RefineConfig()
+
+
+def make_refine_workload(cfg: RefineConfig, n_particles: int, device="cpu", grid: torch.Tensor | None = None):
+    """Particles simulated by the method itself: blob-volume projection at a
+    random pose, sub-pixel shift, defocus offset, CTF, Gaussian noise at a
+    random SNR; starting poses perturbed.  Returns (kwargs, truth)."""
+    rng = np.random.default_rng(cfg.seed + 11)
+    d, H = cfg.template_size, cfg.crop
+    vol, centres = blob_volume(d, cfg.n_blobs, cfg.blob_sigma, cfg.blob_radius, cfg.seed, device=device)
+    template_dft = pp.volume_to_rfft_fourier_slice(vol).cpu().to(torch.complex64)
+    del vol
+    stack, eul0, truth = [], [], []
+    ky = torch.fft.fftfreq(H, dtype=torch.float64)[:, None]
+    kx = torch.fft.rfftfreq(H, dtype=torch.float64)[None, :]
+    for _ in range(n_particles):
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        w, x, y, z = q
+        Rq = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                       [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                       [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+        true_eul = euler_zyz_from_rotmat(Rq)
+        dfo = float(rng.uniform(-cfg.defocus_jitter, cfg.defocus_jitter))
+        shift = rng.uniform(-cfg.shift_px, cfg.shift_px, size=2)
+        snr = float(rng.uniform(*cfg.snr_range))
+        proj = project_blobs(centres, cfg.blob_sigma, Rq, d, device=device).double().cpu()
+        box = torch.zeros(H, H, dtype=torch.float64)
+        o = (H - d) // 2
+        box[o : o + d, o : o + d] = proj
+        f = torch.fft.rfft2(box)
+        f = f * torch.exp(-2j * math.pi * (ky * shift[0] + kx * shift[1]))
+        f = f * pp.ctf_2d((H, H), cfg.defocus + dfo, pixel_size=cfg.pixel_size).double()
+        sig = torch.fft.irfft2(f, s=(H, H))
+        sig = sig - sig.mean()
+        sig = sig * math.sqrt(snr) / sig[o : o + d, o : o + d].std().clamp_min(1e-12)
+        img = torch.randn(H, H, dtype=torch.float64, generator=torch.Generator().manual_seed(int(rng.integers(1 << 30))))
+        img = (img - sig).to(torch.float32)
+        fi = torch.fft.rfftn(img)
+        fi[0, 0] = 0
+        fi = pp.preprocess_image(fi, torch.ones_like(fi.real), torch.ones_like(fi.real), (H, H), (H, H))
+        stack.append(fi.to(torch.complex64))
+        pert = rng.normal(size=3)
+        pert = pert / np.linalg.norm(pert) * rng.uniform(0, cfg.pose_perturbation_deg)
+        eul0.append(true_eul + np.array([pert[0], pert[1], pert[2]]))
+        truth.append(dict(euler=true_eul, defocus_offset=dfo, shift=shift, snr=snr))
+    crop = H - d + 1
+    if grid is None:
+        grid = local_euler_offsets(cfg.grid_angle_range, cfg.grid_angle_step, cfg.grid_angle_range,
+                                   cfg.grid_angle_step)
+    dfs = torch.arange(-cfg.grid_defocus_range, cfg.grid_defocus_range + 1e-6, cfg.grid_defocus_step,
+                       dtype=torch.float32)
+    kwargs = dict(
+        particle_stack_dft=torch.stack(stack),
+        template_dft=template_dft,
+        euler_angles=torch.tensor(np.array(eul0), dtype=torch.float32),
+        euler_angle_offsets=grid,
+        defocus_offsets=dfs,
+        defocus_u=torch.full((n_particles,), cfg.defocus),
+        defocus_v=torch.full((n_particles,), cfg.defocus),
+        defocus_angle=torch.zeros(n_particles),
+        pixel_size_offsets=torch.zeros(1),
+        corr_mean=torch.zeros(n_particles, crop, crop),
+        corr_std=torch.ones(n_particles, crop, crop),
+        ctf_kwargs=dict(voltage=300.0, spherical_aberration=2.7, amplitude_contrast_ratio=0.07, ctf_B_factor=0.0,
+                        phase_shift=0.0, pixel_size=cfg.pixel_size, template_shape=(d, d), even_zernikes=None,
+                        odd_zernikes=None, mag_matrix=None),
+        projective_filters=torch.ones(n_particles, d, d // 2 + 1),
+    )
+    return kwargs, truth
