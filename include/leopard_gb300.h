@@ -200,6 +200,56 @@ int lgb_refine_search(const lgb_refine_problem* problem, const lgb_ctf_params* c
                       int* best_flat, int* best_offset_begin, int* best_batch_len, void* workspace,
                       size_t workspace_bytes, void* stream);
 
+/* ------------------------------------------------------------------------ */
+/* Refinement proposal network (no reference counterpart: Leopard-EM has no  */
+/* learned component; closest analogue core_differentiable_refine.py).       */
+/* Activations and forward weights are BF16 (device), accumulation FP32,     */
+/* gradients FP32.  NCHW; conv weights [Cout][Cin][3][3]; linear [Out][In]. */
+/* ------------------------------------------------------------------------ */
+
+/* y = act(conv3x3(x, w, pad 1, stride 1|2) + b); act = ReLU if relu. */
+int lgb_nn_conv3x3_forward(int N, int Cin, int H, int W, int Cout, int stride, int relu, const void* x,
+                           const void* w, const float* b, void* y, void* stream);
+/* From g = dLoss/d(pre-activation output): dx (optional), dw, db (optional). */
+int lgb_nn_conv3x3_backward(int N, int Cin, int H, int W, int Cout, int stride, const void* x, const void* w,
+                            const float* g, float* dx, float* dw, float* db, void* stream);
+/* y[n][o] = act(sum_i x[n][i] w[o][i] + b[o]) into y_bf16 and/or y_f32. */
+int lgb_nn_linear_forward(int N, int In, int Out, int relu, const void* x, const void* w, const float* b,
+                          void* y_bf16, float* y_f32, void* stream);
+int lgb_nn_linear_backward(int N, int In, int Out, const void* x, const void* w, const float* g, float* dx,
+                           float* dw, float* db, void* stream);
+/* g = dy * (y > 0) for a ReLU output y (bf16). */
+int lgb_nn_relu_backward(long long n, const void* y, const float* dy, float* g, void* stream);
+/* loss = mean_n sum_d w_d (pred - target)^2 and its gradient (weights optional). */
+int lgb_nn_mse(int N, int D, const float* pred, const float* target, const float* weights, float* dpred,
+               float* loss, void* stream);
+/* Adam with bias correction (step >= 1) and decoupled-as-L2 weight decay; also
+ * refreshes the bf16 copy of the parameters when param_bf16 is not NULL. */
+int lgb_nn_adam(long long n, float* param, const float* grad, float* m, float* v, void* param_bf16, float lr,
+                float beta1, float beta2, float eps, float weight_decay, int step, void* stream);
+int lgb_nn_to_bf16(long long n, const float* src, void* dst, void* stream);
+/* Network input per particle p, on the band of `band` x (band/2+1) lowest
+ * frequencies of particle_dft[p] (complex64 [H][W/2+1]); out bf16
+ * [P][6][band][band], band = 64:
+ *   0    the particle band (particle centred in its crop), moved onto the
+ *        reference by the peak of their band cross-correlation, standardised;
+ *   1    the template's central slice at rotations[p] (row-major 3x3) on the
+ *        same physical frequencies times the particle's CTF (the reference);
+ *   2-4  finite-difference derivatives of the reference for 1-degree rotations
+ *        about the image x, y, z axes;
+ *   5    derivative of the reference with respect to defocus (per 100 A);
+ *   channels 1-5 mean-subtracted and scaled by the reference's std;
+ *   out has out_channels >= 6 channels per particle (channels 0-5 written). */
+int lgb_nn_make_inputs(int n_particles, int image_h, int image_w, const void* particle_dft,
+                       const void* template_dft, int template_size, const float* rotations,
+                       const float* defocus_u, const float* defocus_v, const float* defocus_angle,
+                       const lgb_ctf_params* ctf, int band, int out_channels, void* out, void* stream);
+/* Gauss-Newton step from input channels 0-5 (out [P][channels][band][band]):
+ * gn[p][0..7] = (shift x, y in band pixels, rotation about x, y, z in degrees,
+ * defocus in 100 A, amplitude <P,R>/<R,R>, residual fraction); with
+ * channels >= 12 also writes channels 6-11 as constant maps of the step. */
+int lgb_nn_gauss_newton(int n_particles, int band, int channels, void* inputs, float* gn, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

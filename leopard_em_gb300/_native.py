@@ -88,6 +88,16 @@ _SIGNATURES = {
     "lgb_refine_supported": ([ctypes.POINTER(RefineProblem)], _I),
     "lgb_refine_workspace_size": ([ctypes.POINTER(RefineProblem), ctypes.POINTER(_SZ)], _I),
     "lgb_refine_search": ([ctypes.POINTER(RefineProblem), ctypes.POINTER(CtfParams)] + [_P] * 18 + [_SZ, _P], _I),
+    "lgb_nn_conv3x3_forward": ([_I] * 7 + [_P] * 4 + [_P], _I),
+    "lgb_nn_conv3x3_backward": ([_I] * 6 + [_P] * 6 + [_P], _I),
+    "lgb_nn_linear_forward": ([_I] * 4 + [_P] * 5 + [_P], _I),
+    "lgb_nn_linear_backward": ([_I] * 3 + [_P] * 6 + [_P], _I),
+    "lgb_nn_relu_backward": ([_LL, _P, _P, _P, _P], _I),
+    "lgb_nn_mse": ([_I, _I] + [_P] * 5 + [_P], _I),
+    "lgb_nn_adam": ([_LL] + [_P] * 5 + [ctypes.c_float] * 5 + [_I, _P], _I),
+    "lgb_nn_to_bf16": ([_LL, _P, _P, _P], _I),
+    "lgb_nn_make_inputs": ([_I, _I, _I, _P, _P, _I] + [_P] * 4 + [ctypes.POINTER(CtfParams), _I, _I, _P, _P], _I),
+    "lgb_nn_gauss_newton": ([_I, _I, _I, _P, _P, _P], _I),
     "lgb_match_finalize": ([_PROB, _LL, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
 }
 

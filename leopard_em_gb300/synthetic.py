@@ -226,49 +226,100 @@ class RefineConfig:
 CONFIG_REFINE = RefineConfig()
 
 
-def make_refine_workload(cfg: RefineConfig, n_particles: int, device="cpu", grid: torch.Tensor | None = None):
-    """Particles simulated by the method itself: blob-volume projection at a
-    random pose, sub-pixel shift, defocus offset, CTF, Gaussian noise at a
-    random SNR; starting poses perturbed.  Returns (kwargs, truth)."""
-    rng = np.random.default_rng(cfg.seed + 11)
+def random_rotations(n: int, gen: torch.Generator) -> torch.Tensor:
+    """(n, 3, 3) float64 rotations, uniform on SO(3) (unit quaternions)."""
+    q = torch.randn(n, 4, generator=gen, dtype=torch.float64)
+    q = q / q.norm(dim=1, keepdim=True)
+    w, x, y, z = q.unbind(1)
+    return torch.stack([
+        1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w),
+        2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w),
+        2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y),
+    ], dim=1).reshape(n, 3, 3)
+
+
+def axis_angle_rotations(axes: torch.Tensor, angles_rad: torch.Tensor) -> torch.Tensor:
+    a = axes / axes.norm(dim=1, keepdim=True)
+    K = torch.zeros(a.shape[0], 3, 3, dtype=a.dtype)
+    K[:, 0, 1], K[:, 0, 2], K[:, 1, 0] = -a[:, 2], a[:, 1], a[:, 2]
+    K[:, 1, 2], K[:, 2, 0], K[:, 2, 1] = -a[:, 0], -a[:, 1], a[:, 0]
+    s, c = angles_rad.sin()[:, None, None], angles_rad.cos()[:, None, None]
+    return torch.eye(3, dtype=a.dtype) + s * K + (1 - c) * (K @ K)
+
+
+def simulate_particles(cfg: "RefineConfig", centres: np.ndarray, n: int, seed: int, device="cpu", chunk: int = 32):
+    """Particles the method simulates: exact blob-volume projection at a random
+    pose R_true, sub-pixel shift, defocus offset ddf, CTF, additive N(0,1)
+    noise at a random SNR (signal variance / noise variance over the d x d box),
+    contrast inverted, preprocessed like the search input.  Starting poses
+    R_start = D^T R_true with D a rotation by U(0, max) degrees about a random
+    axis.  Returns a dict of tensors (particle_dft on `device`, the rest CPU)."""
+    gen = torch.Generator().manual_seed(seed)
+    d, H = cfg.template_size, cfg.crop
+    o = (H - d) // 2
+    r_true = random_rotations(n, gen)
+    axes = torch.randn(n, 3, generator=gen, dtype=torch.float64)
+    ang = torch.rand(n, generator=gen, dtype=torch.float64) * math.radians(cfg.pose_perturbation_deg)
+    dmat = axis_angle_rotations(axes, ang)
+    r_start = dmat.transpose(1, 2) @ r_true
+    ddf = (torch.rand(n, generator=gen, dtype=torch.float64) * 2 - 1) * cfg.defocus_jitter
+    shift = (torch.rand(n, 2, generator=gen, dtype=torch.float64) * 2 - 1) * cfg.shift_px
+    lo, hi = cfg.snr_range
+    snr = lo + (hi - lo) * torch.rand(n, generator=gen, dtype=torch.float64)
+    noise_seeds = torch.randint(0, 1 << 30, (n,), generator=gen)
+    dev = torch.device(device)
+    cen = torch.tensor(centres, dtype=torch.float32, device=dev)
+    g1 = torch.arange(d, dtype=torch.float32, device=dev) - d // 2
+    ky = (torch.fft.fftfreq(H, dtype=torch.float64, device=dev)[:, None] / cfg.pixel_size)
+    kx = (torch.fft.rfftfreq(H, dtype=torch.float64, device=dev)[None, :] / cfg.pixel_size)
+    k2 = kx**2 + ky**2
+    lam = pp.electron_wavelength(300.0)
+    k5 = math.atan(0.07 / math.sqrt(1 - 0.07**2))
+    chi_static = 0.5 * math.pi * 2.7e7 * lam**3 * k2**2 - k5
+    amp = math.sqrt(2 * math.pi) * cfg.blob_sigma
+    out = torch.empty((n, H, H // 2 + 1), dtype=torch.complex64, device=dev)
+    for a in range(0, n, chunk):
+        b = min(n, a + chunk)
+        R = r_true[a:b].to(dev, torch.float32)
+        pxy = cen[None] @ R                       # (m, nb, 3): rows (R^T c)^T
+        gx = torch.exp(-((g1[None, None, :] - pxy[:, :, 0:1]) ** 2) / (2 * cfg.blob_sigma**2))
+        gy = torch.exp(-((g1[None, None, :] - pxy[:, :, 1:2]) ** 2) / (2 * cfg.blob_sigma**2))
+        proj = amp * (gy.transpose(1, 2) @ gx)    # (m, d, d)
+        box = torch.zeros((b - a, H, H), dtype=torch.float32, device=dev)
+        box[:, o : o + d, o : o + d] = proj
+        f = torch.fft.rfft2(box.double())
+        sh = shift[a:b].to(dev)
+        f = f * torch.exp(-2j * math.pi * (ky[None] * sh[:, 0, None, None] + kx[None] * sh[:, 1, None, None]))
+        df = (cfg.defocus + ddf[a:b]).to(dev)
+        chi = -math.pi * lam * k2[None] * df[:, None, None] + chi_static[None]
+        f = f * (-torch.sin(chi))
+        sig = torch.fft.irfft2(f, s=(H, H))
+        sig = sig - sig.mean(dim=(1, 2), keepdim=True)
+        sd = sig[:, o : o + d, o : o + d].std(dim=(1, 2), keepdim=True).clamp_min(1e-12)
+        sig = sig * (snr[a:b].to(dev).sqrt()[:, None, None] / sd)
+        ngen = torch.Generator(device=dev).manual_seed(int(noise_seeds[a]))
+        noise = torch.randn((b - a, H, H), generator=ngen, dtype=torch.float64, device=dev)
+        img = (noise - sig).to(torch.float32)
+        fi = torch.fft.rfftn(img, dim=(1, 2))
+        fi[:, 0, 0] = 0
+        sq = fi.abs() ** 2
+        ssum = sq.sum(dim=(1, 2), keepdim=True) + sq[:, :, 1:-1].sum(dim=(1, 2), keepdim=True)
+        dim_ = H * (H // 2 + 1) + H * (H // 2 - 1)  # all-ones bandpass dimensionality
+        out[a:b] = (fi / torch.sqrt(ssum) * math.sqrt(dim_)).to(torch.complex64)
+    return {"particle_dft": out, "r_true": r_true, "r_start": r_start, "ddf": ddf, "shift": shift, "snr": snr}
+
+
+def make_refine_workload(cfg: "RefineConfig", n_particles: int, device="cpu", grid: torch.Tensor | None = None,
+                         seed_offset: int = 0):
+    """``core_refine_template`` keyword arguments for n simulated particles
+    (starting poses perturbed, defocus at the nominal value), plus the truth."""
+    from .rotations import rotmat_to_euler_zyz
+
     d, H = cfg.template_size, cfg.crop
     vol, centres = blob_volume(d, cfg.n_blobs, cfg.blob_sigma, cfg.blob_radius, cfg.seed, device=device)
     template_dft = pp.volume_to_rfft_fourier_slice(vol).cpu().to(torch.complex64)
     del vol
-    stack, eul0, truth = [], [], []
-    ky = torch.fft.fftfreq(H, dtype=torch.float64)[:, None]
-    kx = torch.fft.rfftfreq(H, dtype=torch.float64)[None, :]
-    for _ in range(n_particles):
-        q = rng.normal(size=4)
-        q /= np.linalg.norm(q)
-        w, x, y, z = q
-        Rq = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
-                       [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
-                       [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
-        true_eul = euler_zyz_from_rotmat(Rq)
-        dfo = float(rng.uniform(-cfg.defocus_jitter, cfg.defocus_jitter))
-        shift = rng.uniform(-cfg.shift_px, cfg.shift_px, size=2)
-        snr = float(rng.uniform(*cfg.snr_range))
-        proj = project_blobs(centres, cfg.blob_sigma, Rq, d, device=device).double().cpu()
-        box = torch.zeros(H, H, dtype=torch.float64)
-        o = (H - d) // 2
-        box[o : o + d, o : o + d] = proj
-        f = torch.fft.rfft2(box)
-        f = f * torch.exp(-2j * math.pi * (ky * shift[0] + kx * shift[1]))
-        f = f * pp.ctf_2d((H, H), cfg.defocus + dfo, pixel_size=cfg.pixel_size).double()
-        sig = torch.fft.irfft2(f, s=(H, H))
-        sig = sig - sig.mean()
-        sig = sig * math.sqrt(snr) / sig[o : o + d, o : o + d].std().clamp_min(1e-12)
-        img = torch.randn(H, H, dtype=torch.float64, generator=torch.Generator().manual_seed(int(rng.integers(1 << 30))))
-        img = (img - sig).to(torch.float32)
-        fi = torch.fft.rfftn(img)
-        fi[0, 0] = 0
-        fi = pp.preprocess_image(fi, torch.ones_like(fi.real), torch.ones_like(fi.real), (H, H), (H, H))
-        stack.append(fi.to(torch.complex64))
-        pert = rng.normal(size=3)
-        pert = pert / np.linalg.norm(pert) * rng.uniform(0, cfg.pose_perturbation_deg)
-        eul0.append(true_eul + np.array([pert[0], pert[1], pert[2]]))
-        truth.append(dict(euler=true_eul, defocus_offset=dfo, shift=shift, snr=snr))
+    sim = simulate_particles(cfg, centres, n_particles, cfg.seed + 11 + seed_offset, device=device)
     crop = H - d + 1
     if grid is None:
         grid = local_euler_offsets(cfg.grid_angle_range, cfg.grid_angle_step, cfg.grid_angle_range,
@@ -276,9 +327,9 @@ def make_refine_workload(cfg: RefineConfig, n_particles: int, device="cpu", grid
     dfs = torch.arange(-cfg.grid_defocus_range, cfg.grid_defocus_range + 1e-6, cfg.grid_defocus_step,
                        dtype=torch.float32)
     kwargs = dict(
-        particle_stack_dft=torch.stack(stack),
+        particle_stack_dft=sim["particle_dft"].cpu(),
         template_dft=template_dft,
-        euler_angles=torch.tensor(np.array(eul0), dtype=torch.float32),
+        euler_angles=rotmat_to_euler_zyz(sim["r_start"]).to(torch.float32),
         euler_angle_offsets=grid,
         defocus_offsets=dfs,
         defocus_u=torch.full((n_particles,), cfg.defocus),
@@ -292,4 +343,6 @@ def make_refine_workload(cfg: RefineConfig, n_particles: int, device="cpu", grid
                         odd_zernikes=None, mag_matrix=None),
         projective_filters=torch.ones(n_particles, d, d // 2 + 1),
     )
+    truth = {k: v for k, v in sim.items() if k != "particle_dft"}
+    truth["centres"] = centres
     return kwargs, truth
