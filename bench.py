@@ -195,6 +195,7 @@ def refine_bench(args, dev, with_cpu):
         "mean_refined_snr": float(res["refined_z_score"].mean()),
         "workload": cfg.name,
     }
+    out.update(learned_refine_bench(kw, dev, cfg, res, n))
     if with_cpu:
         from oracle import ref_refine_template as orr
 
@@ -208,6 +209,42 @@ def refine_bench(args, dev, with_cpu):
         cpu_s = (time.perf_counter() - t0) * K / m
         out["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": "particles/s", "cores": os.cpu_count() or 1,
                                "kind": "port", "sample": f"1 particle x {m} offsets x {D} defocus, extrapolated to {K} offsets"}
+    return out
+
+
+def learned_refine_bench(kw, dev, cfg, plain_res, n_plain):
+    """Learned proposals + small local grid (fallback: full plain grid) on the
+    same particles as the plain grid, and its throughput on a larger set."""
+    from leopard_em_gb300 import proposal as pr
+    from leopard_em_gb300 import synthetic as sy
+
+    path = os.path.join(ROOT, "leopard_em_gb300", "weights", "proposal_refine288.npz")
+    if not os.path.exists(path):
+        return {"learned": None}
+    net = pr.ProposalNet(dev)
+    pr.load_weights(net, path)
+    small = sy.local_euler_offsets(0.75, 0.25, 0.75, 0.25)
+    small_df = torch.arange(-100.0, 100.0 + 1e-6, 50.0)
+    res, info = pr.refine_with_proposals(net, kw, dev, small, small_df, batch_size=cfg.batch)
+    out = {"learned_mean_refined_snr": float(res["refined_z_score"].mean()),
+           "learned_fallbacks_on_compared": info["fallback"]}
+    n_big = 128
+    kw_big, _ = sy.make_refine_workload(cfg, n_big, device=dev, seed_offset=12345)
+    pr.refine_with_proposals(net, {k: (v[:8] if isinstance(v, torch.Tensor) and v.shape[:1] == (n_big,) else v)
+                                   for k, v in kw_big.items()}, dev, small, small_df, batch_size=cfg.batch)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    res_big, info_big = pr.refine_with_proposals(net, kw_big, dev, small, small_df, batch_size=cfg.batch)
+    torch.cuda.synchronize(dev)
+    dt = time.perf_counter() - t0
+    out["learned"] = {"metric": "refined particles/s (learned proposal + local grid, full-grid fallback)",
+                      "value": n_big / dt, "unit": "particles/s", "particles": n_big,
+                      "fallbacks": info_big["fallback"],
+                      "correlations_per_particle": info_big["correlations_per_particle"],
+                      "mean_refined_snr": float(res_big["refined_z_score"].mean()),
+                      "small_grid": "+-0.75 deg @ 0.25 x +-100 A @ 50",
+                      "timing": "wall clock, host tensors in and out (includes network inputs, inference, "
+                                "two refinement calls and any fallback)"}
     return out
 
 
