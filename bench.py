@@ -58,7 +58,7 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--config", choices=["production", "small"], default="production")
     ap.add_argument("--batch", type=int, default=0, help="orientation batch (0: the configuration's)")
-    ap.add_argument("--refine-particles", type=int, default=4)
+    ap.add_argument("--refine-particles", type=int, default=8)
     ap.add_argument("--no-refine", action="store_true")
     return ap.parse_args()
 
@@ -223,7 +223,7 @@ def learned_refine_bench(kw, dev, cfg, plain_res, n_plain):
         return {"learned": None}
     net = pr.ProposalNet(dev)
     pr.load_weights(net, path)
-    small = sy.local_euler_offsets(0.75, 0.25, 0.75, 0.25)
+    small = sy.local_euler_offsets(1.0, 0.25, 1.0, 0.25)
     small_df = torch.arange(-100.0, 100.0 + 1e-6, 50.0)
     res, info = pr.refine_with_proposals(net, kw, dev, small, small_df, batch_size=cfg.batch)
     out = {"learned_mean_refined_snr": float(res["refined_z_score"].mean()),
@@ -242,7 +242,7 @@ def learned_refine_bench(kw, dev, cfg, plain_res, n_plain):
                       "fallbacks": info_big["fallback"],
                       "correlations_per_particle": info_big["correlations_per_particle"],
                       "mean_refined_snr": float(res_big["refined_z_score"].mean()),
-                      "small_grid": "+-0.75 deg @ 0.25 x +-100 A @ 50",
+                      "small_grid": "+-1 deg @ 0.25 x +-100 A @ 50",
                       "timing": "wall clock, host tensors in and out (includes network inputs, inference, "
                                 "two refinement calls and any fallback)"}
     return out
