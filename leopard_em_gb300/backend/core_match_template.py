@@ -175,6 +175,19 @@ class MatchTemplateSearch:
             )
         self.orientations_done += end - begin
 
+    def maps(self) -> dict:
+        """The four running maps (device tensors, shared with the search)."""
+        return {"mip": self.mip, "best_global_index": self.best_index, "correlation_sum": self.corr_sum,
+                "correlation_squared_sum": self.corr_sq_sum}
+
+    def load_maps(self, maps: dict) -> None:
+        """Replace the running maps, e.g. with the reduction of every rank's maps."""
+        with torch.cuda.device(self.device):
+            self.mip.copy_(maps["mip"])
+            self.best_index.copy_(maps["best_global_index"])
+            self.corr_sum.copy_(maps["correlation_sum"])
+            self.corr_sq_sum.copy_(maps["correlation_squared_sum"])
+
     def result(self, to_cpu: bool = True) -> dict:
         """Decode indices and compute mean / std / z-score (process_results.py:67-183)."""
         H, W = self.shape
