@@ -19,6 +19,9 @@
  *                             cross-correlation of cross_correlation.py:13-154
  *                             and do_iteration_statistics_updates
  *                             (backend/utils.py:191-255), fused
+ *   lgb_match_search_graph    the same loop, replayed as a CUDA graph (the
+ *                             reference launches every kernel of every batch
+ *                             from Python, cross_correlation.py:60-154)
  *   lgb_match_finalize        core_match_template.py:337-349 ->
  *                             process_results.py:67-183
  *                             (decode_global_search_index, scale_mip)
@@ -43,13 +46,24 @@ typedef enum lgb_status {
 
 /* Shape of one whole-orientation search (one micrograph). */
 typedef struct lgb_match_problem {
-  int image_h;            /* H: real-space micrograph rows                         */
-  int image_w;            /* W: real-space micrograph columns (even)               */
+  int image_h;            /* H: rows of the correlation grid (image spectrum, maps) */
+  int image_w;            /* W: columns of the correlation grid (even)              */
   int template_size;      /* d: cubic template edge; projections are d x d        */
   int n_pixel_sizes;      /* C: leading axis of the projective-filter stack       */
   int n_defocus;          /* D: second axis of the projective-filter stack        */
   int n_orientations;     /* N: rows of the Euler-angle table                     */
   int orientation_batch;  /* B: orientations correlated per statistics update     */
+  /* Micrograph size when the image was zero padded to the H x W grid (0 = H or
+   * W): projections are normalised for a micrograph_h x micrograph_w image
+   * (utils.py:106-188) and only map rows < micrograph_h are computed.  With
+   * padding, correlations at valid positions (y <= micrograph_h - d,
+   * x <= micrograph_w - d) equal those of the unpadded search. */
+  int micrograph_h;
+  int micrograph_w;
+  /* Column-pass launch shape: split correlograms over CTAs until the grid
+   * covers about col_waves x the SM count (0 = 4).  Results do not depend on
+   * it. */
+  int col_waves;
 } lgb_match_problem;
 
 /* Kernel stages of one orientation batch inside lgb_match_search. */
@@ -81,6 +95,13 @@ int lgb_profile_end(double* stage_ms, long long* stage_launches, int n_stages);
 /* 1 if every FFT length this problem needs is compiled in, else 0. */
 int lgb_match_supported(const lgb_match_problem* problem);
 
+/* Smallest compiled correlation-grid length >= n along an axis (0 = rows,
+ * image_h; 1 = columns, image_w), or 0 if there is none.  A micrograph whose
+ * size is not compiled is searched on the zero-padded grid (see
+ * micrograph_h / micrograph_w).  No reference counterpart: torch.fft accepts
+ * every length. */
+int lgb_match_fft_size(int n, int axis);
+
 /* Bytes of device scratch that lgb_match_search needs for `problem`. */
 int lgb_match_workspace_size(const lgb_match_problem* problem, size_t* bytes);
 
@@ -89,7 +110,8 @@ int lgb_match_init_stats(long long n_pixels, float* mip, int* best_index, double
                          double* corr_sq_sum, void* stream);
 
 /* Copy the image spectrum (device, complex64 [H][W/2+1], row-major) into the
- * workspace's padded layout.  Must precede lgb_match_search on a workspace. */
+ * workspace's padded layout.  Must precede lgb_match_search on a workspace.
+ * For a zero-padded micrograph this is the spectrum of the padded H x W image. */
 int lgb_match_prepare_image(const lgb_match_problem* problem, const void* image_dft, void* workspace,
                             size_t workspace_bytes, void* stream);
 
@@ -113,6 +135,21 @@ int lgb_match_search(const lgb_match_problem* problem, const void* template_dft,
                      const float* euler_angles, int orientation_begin, int orientation_end, float* mip,
                      int* best_index, double* corr_sum, double* corr_sq_sum, void* workspace,
                      size_t workspace_bytes, void* stream);
+
+/* lgb_match_search through a CUDA graph: the kernels of batches_per_graph
+ * orientation batches are captured once (on a private stream) with their
+ * orientation offset read from a cursor in the workspace, and the graph is
+ * replayed on `stream`, each replay advancing the cursor, until fewer than
+ * batches_per_graph full batches remain; the rest runs as in
+ * lgb_match_search.  Same results as lgb_match_search bit for bit.  The host
+ * enqueues ceil(range / (B * batches_per_graph)) graph launches instead of
+ * 6 kernel launches per batch; the graph is destroyed before returning (after
+ * the launches are enqueued).  `stream` must not be capturing. */
+int lgb_match_search_graph(const lgb_match_problem* problem, const void* template_dft,
+                           const float* projective_filters, const float* euler_angles, int orientation_begin,
+                           int orientation_end, int batches_per_graph, float* mip, int* best_index,
+                           double* corr_sum, double* corr_sq_sum, void* workspace, size_t workspace_bytes,
+                           void* stream);
 
 /* lgb_match_search without any device allocation: no reference counterpart
  * (the reference always allocates through PyTorch).  For callers that cannot

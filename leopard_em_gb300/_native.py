@@ -35,6 +35,9 @@ class MatchProblem(ctypes.Structure):
         ("n_defocus", ctypes.c_int),
         ("n_orientations", ctypes.c_int),
         ("orientation_batch", ctypes.c_int),
+        ("micrograph_h", ctypes.c_int),  # 0 = image_h (no zero padding)
+        ("micrograph_w", ctypes.c_int),  # 0 = image_w
+        ("col_waves", ctypes.c_int),  # 0 = default column-pass launch shape
     ]
 
 
@@ -83,6 +86,8 @@ _SIGNATURES = {
     "lgb_match_prepare_image": ([_PROB, _P, _P, _SZ, _P], _I),
     "lgb_match_filters": ([_PROB, _P, _P, _P, _P], _I),
     "lgb_match_search": ([_PROB, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _SZ, _P], _I),
+    "lgb_match_fft_size": ([_I, _I], _I),
+    "lgb_match_search_graph": ([_PROB, _P, _P, _P, _I, _I, _I, _P, _P, _P, _P, _P, _SZ, _P], _I),
     "lgb_static_scratch_capacity": ([], _SZ),
     "lgb_match_search_static_scratch": ([_PROB, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P], _I),
     "lgb_refine_supported": ([ctypes.POINTER(RefineProblem)], _I),

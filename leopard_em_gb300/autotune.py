@@ -1,0 +1,162 @@
+"""Autotuner for the launch parameters of the whole-orientation search.
+
+Two parameters change the speed of ``lgb_match_search`` but not its results:
+the orientation batch B (correlograms per statistics update: larger batches
+amortise the image-spectrum read and the map read-modify-write over more
+correlograms, at the cost of a larger intermediate) and the column pass's
+grid split (``col_waves``: how many waves of CTAs the correlogram loop is
+split into).  ``tune_search`` times candidates on the caller's own inputs with
+CUDA events, by coordinate descent (B first at the default split, then the
+split at the best B), and caches the winner per device and search shape in a
+JSON file (``$LEOPARD_EM_GB300_TUNE_CACHE``, default
+``~/.cache/leopard_em_gb300/autotune.json``).  The reference has no
+counterpart: its orientation batch is a user setting
+(``ComputationalConfigMatch.batch_size``).
+"""
+
+from __future__ import annotations
+
+import json
+import os
+import threading
+from dataclasses import asdict, dataclass
+
+import torch
+
+from ._native import lib
+
+CACHE_ENV = "LEOPARD_EM_GB300_TUNE_CACHE"
+DEFAULT_BATCHES = (2, 4, 8, 12, 16)
+DEFAULT_WAVES = (2, 4, 8)
+_lock = threading.Lock()
+
+
+@dataclass
+class SearchTuning:
+    orientation_batch: int
+    col_waves: int
+    graph_batches: int
+    ms_per_orientation: float
+
+    @staticmethod
+    def graph_batches_for(batch: int, orientations_per_graph: int = 128) -> int:
+        """Batches per CUDA-graph replay: about ``orientations_per_graph`` orientations."""
+        return max(1, orientations_per_graph // batch)
+
+
+def cache_path() -> str:
+    return os.environ.get(CACHE_ENV) or os.path.join(os.path.expanduser("~"), ".cache", "leopard_em_gb300",
+                                                     "autotune.json")
+
+
+def _load_cache(path: str) -> dict:
+    try:
+        with open(path) as f:
+            data = json.load(f)
+        return data if isinstance(data, dict) else {}
+    except (OSError, ValueError):
+        return {}
+
+
+def _store_cache(path: str, key: str, value: dict) -> None:
+    with _lock:
+        data = _load_cache(path)
+        data[key] = value
+        try:
+            os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
+            tmp = f"{path}.{os.getpid()}.tmp"
+            with open(tmp, "w") as f:
+                json.dump(data, f, indent=1, sort_keys=True)
+            os.replace(tmp, path)
+        except OSError:
+            pass  # a read-only home directory only costs a re-tune
+
+
+def tuning_key(device: torch.device, grid: tuple[int, int], micrograph: tuple[int, int], template_size: int,
+               n_pixel_sizes: int, n_defocus: int) -> str:
+    name = torch.cuda.get_device_name(device).replace(" ", "_")
+    return (f"{name}/v{lib().lgb_version()}/grid{grid[0]}x{grid[1]}/mic{micrograph[0]}x{micrograph[1]}"
+            f"/d{template_size}/C{n_pixel_sizes}/D{n_defocus}")
+
+
+def _time_candidate(make_search, batch: int, waves: int, n_probe: int, repeats: int) -> float:
+    search = make_search(batch, waves)
+    stream = torch.cuda.current_stream(search.device)
+    search.run(0, min(n_probe, batch))  # warm-up: first launches, lazy module loading
+    best = float("inf")
+    for _ in range(repeats):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        search.run(0, n_probe)
+        b.record(stream)
+        b.synchronize()
+        best = min(best, a.elapsed_time(b))
+    del search
+    return best / n_probe
+
+
+def tune_search(image_dft, template_dft, ctf_filters, whitening_filter_template, defocus_values, pixel_values,
+                euler_angles, device, batches=DEFAULT_BATCHES, waves=DEFAULT_WAVES, n_probe: int = 48,
+                repeats: int = 2, memory_fraction: float = 0.5, use_cache: bool = True) -> SearchTuning:
+    """Pick the orientation batch and column split for this search shape.
+
+    Candidates whose workspace would exceed ``memory_fraction`` of the free
+    device memory are skipped.  Probes search the first ``n_probe``
+    orientations into scratch maps (the caller's maps are not touched).
+    """
+    from .backend.core_match_template import MatchTemplateSearch, _single_cuda_device, padded_grid
+
+    dev = _single_cuda_device(device)
+    H, wc = image_dft.shape
+    W = 2 * (wc - 1)
+    d = int(template_dft.shape[0])
+    C, D = int(pixel_values.shape[0]), int(defocus_values.shape[0])
+    grid = padded_grid(H, W)
+    key = tuning_key(dev, grid, (H, W), d, C, D)
+    path = cache_path()
+    if use_cache:
+        hit = _load_cache(path).get(key)
+        if hit:
+            try:
+                return SearchTuning(**hit)
+            except TypeError:
+                pass
+    n_probe = max(1, min(int(n_probe), int(euler_angles.shape[0])))
+    with torch.cuda.device(dev):
+        # device-resident inputs once, so every candidate shares them
+        inputs = dict(
+            image_dft=image_dft.to(dev), template_dft=template_dft.to(dev), ctf_filters=ctf_filters.to(dev),
+            whitening_filter_template=whitening_filter_template.to(dev), defocus_values=defocus_values.to(dev),
+            pixel_values=pixel_values.to(dev), euler_angles=euler_angles[:n_probe].to(dev),
+        )
+        free = torch.cuda.mem_get_info(dev)[0]
+
+        def make_search(batch, w):
+            return MatchTemplateSearch(**inputs, device=dev, orientation_batch_size=batch, col_waves=w)
+
+        def fits(batch):
+            from ._native import MatchProblem
+            import ctypes
+
+            p = MatchProblem(grid[0], grid[1], d, C, D, n_probe, batch, H, W, 0)
+            need = ctypes.c_size_t(0)
+            if lib().lgb_match_workspace_size(ctypes.byref(p), ctypes.byref(need)) != 0:
+                return False
+            return need.value <= memory_fraction * free
+
+        cands = [b for b in batches if b >= 1 and fits(b)] or [1]
+        default_waves = 4 if 4 in waves else waves[0]
+        timings = {}
+        for b in cands:
+            timings[(b, default_waves)] = _time_candidate(make_search, b, default_waves, n_probe, repeats)
+        best_b = min(cands, key=lambda b: timings[(b, default_waves)])
+        for w in waves:
+            if (best_b, w) not in timings:
+                timings[(best_b, w)] = _time_candidate(make_search, best_b, w, n_probe, repeats)
+        (b, w), ms = min(timings.items(), key=lambda kv: kv[1])
+    tuning = SearchTuning(orientation_batch=b, col_waves=w, graph_batches=SearchTuning.graph_batches_for(b),
+                          ms_per_orientation=float(ms))
+    if use_cache:
+        _store_cache(path, key, asdict(tuning))
+    return tuning

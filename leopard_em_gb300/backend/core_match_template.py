@@ -14,10 +14,16 @@ Semantics kept from the reference:
     a batch (backend/utils.py:241-252);
   * decode and z-score scaling of process_results.py:67-183, including the
     "correlation_variance" key holding the standard deviation.
-Deliberate differences (documented in the design doc):
+Deliberate differences:
   * sums and sums of squares accumulate in FP64 (reference: FP32);
   * the last, partial orientation batch is indexed correctly (the reference
-    always builds a full-length index vector, :513-520).
+    always builds a full-length index vector, :513-520);
+  * a micrograph whose height or width is not a compiled FFT length is
+    searched on the next compiled grid with zero padding.  Correlations at
+    valid positions (y <= H - d, x <= W - d) are those of the unpadded
+    search; in the margin the reference's circular wrap-around becomes a
+    linear correlation (the manager crops that margin,
+    match_template_result.py apply_valid_cropping).
 """
 
 from __future__ import annotations
@@ -46,7 +52,20 @@ def _single_cuda_device(device) -> torch.device:
 
 
 def _ptr(t: torch.Tensor) -> int:
+    """Device address of a tensor handed to the C ABI (dense row-major only)."""
+    if not t.is_contiguous():
+        raise ValueError(f"tensor of shape {tuple(t.shape)} is not contiguous; the C ABI takes row-major buffers")
     return t.data_ptr()
+
+
+def padded_grid(h: int, w: int) -> tuple[int, int]:
+    """Correlation grid for an h x w micrograph: the smallest compiled FFT
+    lengths >= h and >= w (equal to (h, w) when both are compiled)."""
+    L = lib()
+    hp, wp = int(L.lgb_match_fft_size(int(h), 0)), int(L.lgb_match_fft_size(int(w), 1))
+    if hp == 0 or wp == 0:
+        raise ValueError(f"no compiled FFT grid holds a {h}x{w} micrograph")
+    return hp, wp
 
 
 class MatchTemplateSearch:
@@ -69,7 +88,12 @@ class MatchTemplateSearch:
         euler_angles: torch.Tensor,
         device,
         orientation_batch_size: int = 1,
+        graph_batches: int = 0,
+        col_waves: int = 0,
     ):
+        """``graph_batches`` > 0 replays that many orientation batches per CUDA
+        graph launch (``lgb_match_search_graph``); ``col_waves`` sets the column
+        pass launch shape (0 = default).  Neither changes any result."""
         self.device = _single_cuda_device(device)
         if image_dft.dim() != 2 or template_dft.dim() != 3:
             raise ValueError("image_dft must be (H, W//2+1) and template_dft (d, d, d//2+1)")
@@ -90,19 +114,27 @@ class MatchTemplateSearch:
             raise ValueError("euler_angles must be (N, 3)")
         if orientation_batch_size < 1:
             raise ValueError("orientation_batch_size must be >= 1")
+        if graph_batches < 0 or col_waves < 0:
+            raise ValueError("graph_batches and col_waves must be >= 0")
+        L = lib()
+        Hp, Wp = padded_grid(H, W)
         self.problem = MatchProblem(
-            image_h=H,
-            image_w=W,
+            image_h=Hp,
+            image_w=Wp,
             template_size=d,
             n_pixel_sizes=n_cs,
             n_defocus=n_df,
             n_orientations=int(euler_angles.shape[0]),
             orientation_batch=int(orientation_batch_size),
+            micrograph_h=H,
+            micrograph_w=W,
+            col_waves=int(col_waves),
         )
-        L = lib()
+        self.graph_batches = int(graph_batches)
         if not L.lgb_match_supported(ctypes.byref(self.problem)):
             raise ValueError(
-                f"unsupported search shape: image {H}x{W}, template {d} (FFT lengths outside the compiled set)"
+                f"unsupported search shape: image {H}x{W} (grid {Hp}x{Wp}), template {d} "
+                "(FFT lengths outside the compiled set)"
             )
         dev = self.device
         with torch.cuda.device(dev):
@@ -110,6 +142,12 @@ class MatchTemplateSearch:
             self._stream = stream
             s = ctypes.c_void_p(stream.cuda_stream)
             self.image_dft = image_dft.to(dev, torch.complex64, non_blocking=True).contiguous()
+            if (Hp, Wp) != (H, W):
+                # spectrum of the zero-padded micrograph (set-up, once per micrograph)
+                img = torch.fft.irfftn(self.image_dft, s=(H, W))
+                # (cuFFT returns the 2-D transform with transposed strides)
+                self.image_dft = torch.fft.rfftn(torch.nn.functional.pad(img, (0, Wp - W, 0, Hp - H))).contiguous()
+                del img
             self.template_dft = template_dft.to(dev, torch.complex64, non_blocking=True).contiguous()
             self.euler_angles = euler_angles.to(dev, torch.float32, non_blocking=True).contiguous()
             self.defocus_values = defocus_values.to(dev, torch.float32, non_blocking=True).contiguous()
@@ -124,13 +162,13 @@ class MatchTemplateSearch:
             nbytes = ctypes.c_size_t(0)
             check(L.lgb_match_workspace_size(ctypes.byref(self.problem), ctypes.byref(nbytes)), "workspace size")
             self.workspace = torch.empty(int(nbytes.value), dtype=torch.uint8, device=dev)
-            self.mip = torch.empty((H, W), dtype=torch.float32, device=dev)
-            self.best_index = torch.empty((H, W), dtype=torch.int32, device=dev)
-            self.corr_sum = torch.empty((H, W), dtype=torch.float64, device=dev)
-            self.corr_sq_sum = torch.empty((H, W), dtype=torch.float64, device=dev)
+            self.mip = torch.empty((Hp, Wp), dtype=torch.float32, device=dev)
+            self.best_index = torch.empty((Hp, Wp), dtype=torch.int32, device=dev)
+            self.corr_sum = torch.empty((Hp, Wp), dtype=torch.float64, device=dev)
+            self.corr_sq_sum = torch.empty((Hp, Wp), dtype=torch.float64, device=dev)
             check(
                 L.lgb_match_init_stats(
-                    H * W, _ptr(self.mip), _ptr(self.best_index), _ptr(self.corr_sum), _ptr(self.corr_sq_sum), s
+                    Hp * Wp, _ptr(self.mip), _ptr(self.best_index), _ptr(self.corr_sum), _ptr(self.corr_sq_sum), s
                 ),
                 "lgb_match_init_stats",
             )
@@ -141,12 +179,21 @@ class MatchTemplateSearch:
                 "lgb_match_prepare_image",
             )
         self.shape = (H, W)
+        self.grid = (Hp, Wp)
         self.orientations_done = 0
 
     @property
     def total_projections(self) -> int:
         p = self.problem
         return p.n_orientations * p.n_defocus * p.n_pixel_sizes
+
+    @property
+    def searched_projections(self) -> int:
+        """Correlograms folded into the maps so far (the mean / std divisor;
+        equal to ``total_projections`` once every orientation has run)."""
+        p = self.problem
+        done = self.orientations_done if self.orientations_done > 0 else p.n_orientations
+        return done * p.n_defocus * p.n_pixel_sizes
 
     def run(self, begin: int = 0, end: int | None = None) -> None:
         """Correlate orientations [begin, end) and fold them into the maps."""
@@ -155,6 +202,17 @@ class MatchTemplateSearch:
             raise ValueError(f"orientation range [{begin}, {end}) outside [0, {self.problem.n_orientations})")
         with torch.cuda.device(self.device):
             s = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+            if self.graph_batches > 0:
+                check(
+                    lib().lgb_match_search_graph(
+                        ctypes.byref(self.problem), _ptr(self.template_dft), _ptr(self.projective_filters),
+                        _ptr(self.euler_angles), int(begin), int(end), self.graph_batches, _ptr(self.mip),
+                        _ptr(self.best_index), _ptr(self.corr_sum), _ptr(self.corr_sq_sum), _ptr(self.workspace),
+                        self.workspace.numel(), s),
+                    "lgb_match_search_graph",
+                )
+                self.orientations_done += end - begin
+                return
             check(
                 lib().lgb_match_search(
                     ctypes.byref(self.problem),
@@ -189,18 +247,21 @@ class MatchTemplateSearch:
             self.corr_sq_sum.copy_(maps["correlation_squared_sum"])
 
     def result(self, to_cpu: bool = True) -> dict:
-        """Decode indices and compute mean / std / z-score (process_results.py:67-183)."""
+        """Decode indices and compute mean / std / z-score (process_results.py:67-183).
+
+        Maps are H x W (the micrograph), also when the search ran on a padded grid."""
         H, W = self.shape
+        Hp, Wp = self.grid
         dev = self.device
         with torch.cuda.device(dev):
             s = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
-            out = {k: torch.empty((H, W), dtype=torch.float32, device=dev) for k in
+            out = {k: torch.empty((Hp, Wp), dtype=torch.float32, device=dev) for k in
                    ("scaled_mip", "best_phi", "best_theta", "best_psi", "best_defocus",
                     "correlation_mean", "correlation_variance")}
             check(
                 lib().lgb_match_finalize(
                     ctypes.byref(self.problem),
-                    self.total_projections,
+                    self.searched_projections,
                     _ptr(self.mip),
                     _ptr(self.best_index),
                     _ptr(self.corr_sum),
@@ -228,6 +289,8 @@ class MatchTemplateSearch:
                 "correlation_mean": out["correlation_mean"],
                 "correlation_variance": out["correlation_variance"],
             }
+            if (Hp, Wp) != (H, W):
+                res = {k: v[:H, :W].contiguous() for k, v in res.items()}
             if to_cpu:
                 res = {k: v.cpu() for k, v in res.items()}
         res["total_projections"] = self.total_projections

@@ -10,21 +10,28 @@
 namespace lgb {
 
 struct MatchLayout {
-  size_t ip, slices, t, proj, rowstats, a, y, total;
+  size_t ip, slices, t, proj, rowstats, a, y, cursor, total;
   int wc_img, wcp, wc_t, n_c_max;
 };
 
 static size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
 
+// Micrograph size inside the (possibly zero-padded) correlation grid.
+static int mic_h(const lgb_match_problem* p) { return p->micrograph_h > 0 ? p->micrograph_h : p->image_h; }
+static int mic_w(const lgb_match_problem* p) { return p->micrograph_w > 0 ? p->micrograph_w : p->image_w; }
+
 static bool valid_problem(const lgb_match_problem* p) {
   return p && p->image_h > 0 && p->image_w > 0 && (p->image_w % 2) == 0 && p->template_size > 1 &&
          (p->template_size % 2) == 0 && p->n_pixel_sizes > 0 && p->n_defocus > 0 && p->n_orientations > 0 &&
-         p->orientation_batch > 0 && p->template_size <= p->image_h && p->template_size <= p->image_w;
+         p->orientation_batch > 0 && p->template_size <= p->image_h && p->template_size <= p->image_w &&
+         p->micrograph_h >= 0 && p->micrograph_w >= 0 && p->col_waves >= 0 && mic_h(p) <= p->image_h &&
+         mic_w(p) <= p->image_w && p->template_size <= mic_h(p) && p->template_size <= mic_w(p);
 }
 
 static MatchLayout layout_of(const lgb_match_problem* p) {
   MatchLayout L{};
   const size_t H = p->image_h, W = p->image_w, h = p->template_size;
+  const size_t y_rows = mic_h(p);
   L.wc_img = (int)(W / 2 + 1);
   L.wcp = pad4(L.wc_img);
   L.wc_t = (int)(h / 2 + 1);
@@ -44,7 +51,9 @@ static MatchLayout layout_of(const lgb_match_problem* p) {
   L.a = off;
   off += align256(nc * h * L.wcp * sizeof(float2));
   L.y = off;
-  off += align256(nc * H * L.wcp * sizeof(float2));
+  off += align256(nc * y_rows * L.wcp * sizeof(float2));
+  L.cursor = off;  // orientation cursor of graph replays
+  off += 256;
   L.total = off;
   return L;
 }
@@ -116,8 +125,8 @@ struct StageScope {
   int stage;
   cudaStream_t s;
   cudaEvent_t a = nullptr, b = nullptr;
-  StageScope(int st, cudaStream_t str) : stage(st), s(str) {
-    if (!g_prof_on) return;
+  StageScope(int st, cudaStream_t str, bool on) : stage(st), s(str) {
+    if (!on) return;
     if (cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess) cudaEventRecord(a, s);
   }
   ~StageScope() {
@@ -132,6 +141,94 @@ static int grid_for(long long n) {
   long long g = (n + 255) / 256;
   if (g > 65535LL * 16) g = 65535LL * 16;
   return (int)(g < 1 ? 1 : g);
+}
+
+__global__ void set_cursor_kernel(int* cursor, int value) { *cursor = value; }
+__global__ void advance_cursor_kernel(int* cursor, int step) { *cursor += step; }
+
+// Validated pointers and layout of one search call.
+struct SearchArgs {
+  const lgb_match_problem* p;
+  MatchLayout L;
+  char* ws;
+  const void* template_dft;
+  const float* pf;
+  const float* euler;
+  float* mip;
+  int* best;
+  double* s1;
+  double* s2;
+};
+
+static int search_args(const lgb_match_problem* p, const void* template_dft, const float* pf, const float* euler,
+                       int begin, int end, float* mip, int* best, double* s1, double* s2, void* workspace,
+                       size_t workspace_bytes, SearchArgs* a) {
+  if (!valid_problem(p) || !template_dft || !pf || !euler || !mip || !best || !s1 || !s2 || !workspace)
+    return LGB_ERR_INVALID_ARGUMENT;
+  if (begin < 0 || end > p->n_orientations || begin > end) return LGB_ERR_INVALID_ARGUMENT;
+  if (!lgb_match_supported(p)) return LGB_ERR_UNSUPPORTED_SIZE;
+  const long long total_idx = (long long)p->n_orientations * p->n_defocus * p->n_pixel_sizes;
+  if (total_idx > 2147483647LL) return LGB_ERR_INVALID_ARGUMENT;  // int32 global index, as the reference
+  a->p = p;
+  a->L = layout_of(p);
+  if (workspace_bytes < a->L.total) return LGB_ERR_WORKSPACE_TOO_SMALL;
+  a->ws = static_cast<char*>(workspace);
+  a->template_dft = template_dft;
+  a->pf = pf;
+  a->euler = euler;
+  a->mip = mip;
+  a->best = best;
+  a->s1 = s1;
+  a->s2 = s2;
+  return LGB_OK;
+}
+
+// The six kernels of one orientation batch: orientations o0 (+ *o0_dev when
+// given) .. + nb.  `profile` brackets each launch with the stage profiler's
+// events (off while a graph is being captured).
+static int run_batch(const SearchArgs& a, int o0, const int* o0_dev, int nb, bool profile, cudaStream_t s) {
+  const lgb_match_problem* p = a.p;
+  const MatchLayout& L = a.L;
+  void* ip = a.ws + L.ip;
+  void* slices = a.ws + L.slices;
+  void* T = a.ws + L.t;
+  float* proj = reinterpret_cast<float*>(a.ws + L.proj);
+  double* rowstats = reinterpret_cast<double*>(a.ws + L.rowstats);
+  void* A = a.ws + L.a;
+  void* Y = a.ws + L.y;
+  const int h = p->template_size, H = p->image_h, W = p->image_w;
+  const int y_rows = mic_h(p);
+  const int n_cd = p->n_pixel_sizes * p->n_defocus;
+  const int n_c = n_cd * nb;
+  const bool prof = profile && g_prof_on;
+  int st;
+  {
+    StageScope sc(LGB_STAGE_SLICE, s, prof);
+    if ((st = launch_slice(a.template_dft, h, a.euler, o0, o0_dev, nb, nullptr, slices, s))) return st;
+  }
+  {
+    StageScope sc(LGB_STAGE_PROJ_COL, s, prof);
+    if ((st = launch_proj_col(h, slices, a.pf, nb, n_cd, n_c, T, s))) return st;
+  }
+  {
+    StageScope sc(LGB_STAGE_PROJ_ROW, s, prof);
+    if ((st = launch_proj_row(h, T, n_c, proj, rowstats, s))) return st;
+  }
+  {
+    StageScope sc(LGB_STAGE_PAD_RFFT, s, prof);
+    if ((st = launch_pad_rfft(W, proj, rowstats, h, mic_h(p), mic_w(p), L.wcp, n_c, A, s))) return st;
+  }
+  {
+    StageScope sc(LGB_STAGE_COLPASS, s, prof);
+    if ((st = launch_colpass(H, A, ip, h, L.wcp, n_c, n_c, y_rows, p->col_waves, Y, s))) return st;
+  }
+  {
+    StageScope sc(LGB_STAGE_ROWPASS, s, prof);
+    if ((st = launch_rowpass(W, Y, H, y_rows, L.wcp, n_c, nb, p->n_orientations, o0, o0_dev, a.mip, a.best, a.s1,
+                             a.s2, s)))
+      return st;
+  }
+  return LGB_OK;
 }
 
 }  // namespace lgb
@@ -199,6 +296,13 @@ int lgb_match_supported(const lgb_match_problem* p) {
   return supported_template(p->template_size) && supported_row(p->image_w) && supported_col(p->image_h);
 }
 
+int lgb_match_fft_size(int n, int axis) {
+  if (n < 1 || (axis != 0 && axis != 1)) return 0;
+  for (int m = n; m <= 2 * n + 64; ++m)
+    if (axis == 0 ? supported_col(m) : supported_row(m)) return m;
+  return 0;
+}
+
 int lgb_match_workspace_size(const lgb_match_problem* p, size_t* bytes) {
   if (!valid_problem(p) || !bytes) return LGB_ERR_INVALID_ARGUMENT;
   *bytes = layout_of(p).total;
@@ -240,57 +344,67 @@ int lgb_match_search(const lgb_match_problem* p, const void* template_dft, const
                      const float* euler_angles, int orientation_begin, int orientation_end, float* mip,
                      int* best_index, double* corr_sum, double* corr_sq_sum, void* workspace, size_t workspace_bytes,
                      void* stream) {
-  if (!valid_problem(p) || !template_dft || !projective_filters || !euler_angles || !mip || !best_index ||
-      !corr_sum || !corr_sq_sum || !workspace)
-    return LGB_ERR_INVALID_ARGUMENT;
-  if (orientation_begin < 0 || orientation_end > p->n_orientations || orientation_begin > orientation_end)
-    return LGB_ERR_INVALID_ARGUMENT;
-  if (!lgb_match_supported(p)) return LGB_ERR_UNSUPPORTED_SIZE;
-  const long long total_idx = (long long)p->n_orientations * p->n_defocus * p->n_pixel_sizes;
-  if (total_idx > 2147483647LL) return LGB_ERR_INVALID_ARGUMENT;  // int32 global index, as the reference
-  const MatchLayout L = layout_of(p);
-  if (workspace_bytes < L.total) return LGB_ERR_WORKSPACE_TOO_SMALL;
+  SearchArgs a{};
+  int st = search_args(p, template_dft, projective_filters, euler_angles, orientation_begin, orientation_end, mip,
+                       best_index, corr_sum, corr_sq_sum, workspace, workspace_bytes, &a);
+  if (st != LGB_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
-  char* ws = static_cast<char*>(workspace);
-  void* ip = ws + L.ip;
-  void* slices = ws + L.slices;
-  void* T = ws + L.t;
-  float* proj = reinterpret_cast<float*>(ws + L.proj);
-  double* rowstats = reinterpret_cast<double*>(ws + L.rowstats);
-  void* A = ws + L.a;
-  void* Y = ws + L.y;
-  const int h = p->template_size, H = p->image_h, W = p->image_w;
-  const int n_cd = p->n_pixel_sizes * p->n_defocus;
-  int st;
   for (int o0 = orientation_begin; o0 < orientation_end; o0 += p->orientation_batch) {
     const int nb = (orientation_end - o0) < p->orientation_batch ? (orientation_end - o0) : p->orientation_batch;
-    const int n_c = n_cd * nb;
-    {
-      StageScope sc(LGB_STAGE_SLICE, s);
-      if ((st = launch_slice(template_dft, h, euler_angles, o0, nb, nullptr, slices, s))) return st;
+    if ((st = run_batch(a, o0, nullptr, nb, true, s))) return st;
+  }
+  return LGB_OK;
+}
+
+int lgb_match_search_graph(const lgb_match_problem* p, const void* template_dft, const float* projective_filters,
+                           const float* euler_angles, int orientation_begin, int orientation_end,
+                           int batches_per_graph, float* mip, int* best_index, double* corr_sum,
+                           double* corr_sq_sum, void* workspace, size_t workspace_bytes, void* stream) {
+  if (batches_per_graph < 1) return LGB_ERR_INVALID_ARGUMENT;
+  SearchArgs a{};
+  int st = search_args(p, template_dft, projective_filters, euler_angles, orientation_begin, orientation_end, mip,
+                       best_index, corr_sum, corr_sq_sum, workspace, workspace_bytes, &a);
+  if (st != LGB_OK) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long chunk = (long long)batches_per_graph * p->orientation_batch;
+  const long long replays = (orientation_end - orientation_begin) / chunk;
+  if (replays > 0) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+      return LGB_ERR_INVALID_ARGUMENT;
+    int* cursor = reinterpret_cast<int*>(a.ws + a.L.cursor);
+    cudaStream_t cs = nullptr;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return LGB_ERR_CUDA;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    st = LGB_OK;
+    if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      st = LGB_ERR_CUDA;
+    } else {
+      for (int m = 0; m < batches_per_graph && st == LGB_OK; ++m)
+        st = run_batch(a, m * p->orientation_batch, cursor, p->orientation_batch, false, cs);
+      if (st == LGB_OK) {
+        advance_cursor_kernel<<<1, 1, 0, cs>>>(cursor, (int)chunk);
+        if (cudaGetLastError() != cudaSuccess) st = LGB_ERR_CUDA;
+      }
+      if (cudaStreamEndCapture(cs, &graph) != cudaSuccess && st == LGB_OK) st = LGB_ERR_CUDA;
     }
-    {
-      StageScope sc(LGB_STAGE_PROJ_COL, s);
-      if ((st = launch_proj_col(h, slices, projective_filters, nb, n_cd, n_c, T, s))) return st;
+    if (st == LGB_OK && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) st = LGB_ERR_CUDA;
+    if (st == LGB_OK) {
+      set_cursor_kernel<<<1, 1, 0, s>>>(cursor, orientation_begin);
+      if (cudaGetLastError() != cudaSuccess) st = LGB_ERR_CUDA;
+      for (long long r = 0; r < replays && st == LGB_OK; ++r)
+        if (cudaGraphLaunch(exec, s) != cudaSuccess) st = LGB_ERR_CUDA;
     }
-    {
-      StageScope sc(LGB_STAGE_PROJ_ROW, s);
-      if ((st = launch_proj_row(h, T, n_c, proj, rowstats, s))) return st;
-    }
-    {
-      StageScope sc(LGB_STAGE_PAD_RFFT, s);
-      if ((st = launch_pad_rfft(W, proj, rowstats, h, H, L.wcp, n_c, A, s))) return st;
-    }
-    {
-      StageScope sc(LGB_STAGE_COLPASS, s);
-      if ((st = launch_colpass(H, A, ip, h, L.wcp, n_c, n_c, H, Y, s))) return st;
-    }
-    {
-      StageScope sc(LGB_STAGE_ROWPASS, s);
-      if ((st = launch_rowpass(W, Y, H, L.wcp, n_c, nb, p->n_orientations, o0, mip, best_index, corr_sum,
-                               corr_sq_sum, s)))
-        return st;
-    }
+    // in-flight launches complete before the executable graph is freed
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    if (st != LGB_OK) return st;
+  }
+  for (long long o0 = orientation_begin + replays * chunk; o0 < orientation_end; o0 += p->orientation_batch) {
+    const int nb = (int)((orientation_end - o0) < p->orientation_batch ? (orientation_end - o0) : p->orientation_batch);
+    if ((st = run_batch(a, (int)o0, nullptr, nb, true, s))) return st;
   }
   return LGB_OK;
 }

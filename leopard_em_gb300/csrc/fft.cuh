@@ -259,9 +259,15 @@ LGB_PLAN(512, 8, 8, 8)
 LGB_PLAN(576, 16, 4, 3, 3)
 LGB_PLAN(768, 16, 16, 3)
 LGB_PLAN(1024, 16, 8, 8)
+LGB_PLAN(1440, 16, 5, 3, 3, 2)
 LGB_PLAN(1536, 16, 8, 4, 3)
+LGB_PLAN(1920, 16, 8, 5, 3)
 LGB_PLAN(2048, 8, 16, 16)
+LGB_PLAN(2880, 16, 4, 5, 3, 3)
+LGB_PLAN(3072, 16, 16, 4, 3)
+LGB_PLAN(3840, 16, 16, 5, 3)
 LGB_PLAN(4096, 16, 16, 16)
+LGB_PLAN(5760, 16, 8, 5, 3, 3)
 #undef LGB_PLAN
 
 template <int N, int NT, int DIR, class IDX, int NS, bool PRUNED, class RL>

@@ -6,7 +6,8 @@
 
 namespace lgb {
 
-#define LGB_COL_SIZES(X) X(48) X(64) X(128) X(256) X(288) X(512) X(576) X(1024) X(2048) X(4096)
+#define LGB_COL_SIZES(X) \
+  X(48) X(64) X(128) X(256) X(288) X(512) X(576) X(1024) X(2048) X(2880) X(3072) X(3840) X(4096) X(5760)
 
 bool supported_col(int H) {
   switch (H) {
@@ -19,52 +20,49 @@ bool supported_col(int H) {
   }
 }
 
-template <int HN>
-static int colpass_t(const void* A, const void* Ip, int h, int Wcp, int n_c, int cpi, int y_rows, void* Y,
-                     cudaStream_t s) {
-  constexpr int NT = FftThreads<HN>::value;
-  const size_t smem = sizeof(float2) * kColGroup * (IdxPad16::pad(HN) + 4);
-  if (cudaFuncSetAttribute(colpass_kernel<HN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-      cudaSuccess)
-    return LGB_ERR_CUDA;
+// Split the correlogram loop of each column group over grid.y until the grid
+// covers about `waves` x the SM count; returns the split and the correlograms
+// per CTA.
+static int colpass_split(int groups, int n_c, int waves, int* per) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int groups = Wcp / kColGroup;
-  // split the correlogram loop so that the grid covers at least ~4 waves
+  if (waves <= 0) waves = 4;
   int split = 1;
-  while (split < n_c && groups * split < 4 * sms) split *= 2;
-  if (split > n_c) split = n_c;
-  const int per = (n_c + split - 1) / split;
-  split = (n_c + per - 1) / per;
-  dim3 grid(groups, split);
-  colpass_kernel<HN><<<grid, kColGroup * NT, smem, s>>>(static_cast<const float2*>(A),
-                                                       static_cast<const float2*>(Ip), h, Wcp, n_c, per, cpi,
-                                                       y_rows, static_cast<float2*>(Y));
-  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
-}
-
-static int colpass_split(int groups, int n_c, int* per) {
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int split = 1;
-  while (split < n_c && groups * split < 4 * sms) split *= 2;
+  while (split < n_c && groups * split < waves * sms) split *= 2;
   if (split > n_c) split = n_c;
   *per = (n_c + split - 1) / split;
   return (n_c + *per - 1) / *per;
 }
 
+template <int HN>
+static int colpass_t(const void* A, const void* Ip, int h, int Wcp, int n_c, int cpi, int y_rows, int waves, void* Y,
+                     cudaStream_t s) {
+  constexpr int NT = FftThreads<HN>::value;
+  constexpr int G = ColGroupOf<HN>::value;
+  const size_t smem = sizeof(float2) * G * (IdxPad16::pad(HN) + 4);
+  if (cudaFuncSetAttribute(colpass_kernel<HN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return LGB_ERR_CUDA;
+  int per = 1;
+  const int groups = Wcp / G;
+  const int split = colpass_split(groups, n_c, waves, &per);
+  dim3 grid(groups, split);
+  colpass_kernel<HN><<<grid, G * NT, smem, s>>>(static_cast<const float2*>(A), static_cast<const float2*>(Ip), h, Wcp,
+                                                n_c, per, cpi, y_rows, static_cast<float2*>(Y));
+  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+}
+
 template <int R, int P>
-static int colpass_fused_t(const void* A, const void* Ip, int h, int Wcp, int n_c, int cpi, int y_rows, void* Y,
-                           cudaStream_t s) {
+static int colpass_fused_t(const void* A, const void* Ip, int h, int Wcp, int n_c, int cpi, int y_rows, int waves,
+                           void* Y, cudaStream_t s) {
   using CF = ColFused<R, P>;
   if (cudaFuncSetAttribute(colpass_fused_kernel<R, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF::SMEM) !=
       cudaSuccess)
     return LGB_ERR_CUDA;
   int per = 1;
   const int groups = Wcp / kColGroup;
-  const int split = colpass_split(groups, n_c, &per);
+  const int split = colpass_split(groups, n_c, waves, &per);
   dim3 grid(groups, split);
   colpass_fused_kernel<R, P><<<grid, CF::THREADS, CF::SMEM, s>>>(
       static_cast<const float2*>(A), static_cast<const float2*>(Ip), h, Wcp, n_c, per, cpi, y_rows,
@@ -72,25 +70,25 @@ static int colpass_fused_t(const void* A, const void* Ip, int h, int Wcp, int n_
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
-int launch_colpass(int H, const void* A, const void* Ip, int h, int Wcp, int n_c, int cpi, int y_rows, void* Y,
-                   cudaStream_t s) {
-  if (cpi < 1 || y_rows < 1 || y_rows > H) return LGB_ERR_INVALID_ARGUMENT;
+int launch_colpass(int H, const void* A, const void* Ip, int h, int Wcp, int n_c, int cpi, int y_rows, int waves,
+                   void* Y, cudaStream_t s) {
+  if (cpi < 1 || y_rows < 1 || y_rows > H || Wcp % kColGroup) return LGB_ERR_INVALID_ARGUMENT;
   switch (H) {
     case 4096:
-      return colpass_fused_t<16, 3>(A, Ip, h, Wcp, n_c, cpi, y_rows, Y, s);
+      return colpass_fused_t<16, 3>(A, Ip, h, Wcp, n_c, cpi, y_rows, waves, Y, s);
     case 512:
-      return colpass_fused_t<8, 3>(A, Ip, h, Wcp, n_c, cpi, y_rows, Y, s);
+      return colpass_fused_t<8, 3>(A, Ip, h, Wcp, n_c, cpi, y_rows, waves, Y, s);
     case 256:
-      return colpass_fused_t<16, 2>(A, Ip, h, Wcp, n_c, cpi, y_rows, Y, s);
+      return colpass_fused_t<16, 2>(A, Ip, h, Wcp, n_c, cpi, y_rows, waves, Y, s);
     case 64:
-      return colpass_fused_t<8, 2>(A, Ip, h, Wcp, n_c, cpi, y_rows, Y, s);
+      return colpass_fused_t<8, 2>(A, Ip, h, Wcp, n_c, cpi, y_rows, waves, Y, s);
     default:
       break;
   }
   switch (H) {
 #define X(n) \
   case n:    \
-    return colpass_t<n>(A, Ip, h, Wcp, n_c, cpi, y_rows, Y, s);
+    return colpass_t<n>(A, Ip, h, Wcp, n_c, cpi, y_rows, waves, Y, s);
     LGB_COL_SIZES(X)
 #undef X
     default:

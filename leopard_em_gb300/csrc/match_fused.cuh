@@ -384,9 +384,9 @@ struct RowFused {
 
 template <int WH, int NT, class RL>
 __global__ void __launch_bounds__(NT, 2)
-    rowpass_fused_kernel(const float2* __restrict__ Y, int H, int Wcp, int n_c, int nb, int n_orient, int o0,
-                         float scale, float* __restrict__ mip, int* __restrict__ best, double* __restrict__ s1,
-                         double* __restrict__ s2) {
+    rowpass_fused_kernel(const float2* __restrict__ Y, int y_rows, int Wcp, int n_c, int nb, int n_orient, int o0,
+                         const int* __restrict__ o0_dev, float scale, float* __restrict__ mip,
+                         int* __restrict__ best, double* __restrict__ s1, double* __restrict__ s2) {
   using RF = RowFused<WH, NT, RL>;
   constexpr int R1 = RF::R1, RLAST = RF::RLAST, NB1 = RF::NB1, PER1 = RF::PER1, NBL = RF::NBL, PERL = RF::PERL;
   constexpr int OUT = PERL * RLAST;  // complex outputs (pixel pairs) per thread
@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(NT, 2)
     const float2* xr = (c & 1) ? xr1 : xr0;
     if (c + 1 < n_c) {
       float2* nxt = (c & 1) ? xr0 : xr1;
-      const float2* src = Y + ((size_t)(c + 1) * H + y) * Wcp;
+      const float2* src = Y + ((size_t)(c + 1) * y_rows + y) * Wcp;
       for (int i = t; i < n16; i += NT) cp_async16(nxt + 2 * i, src + 2 * i);
       cp_async_commit();
       cp_async_wait<1>();
@@ -496,6 +496,7 @@ __global__ void __launch_bounds__(NT, 2)
   }
 
   const size_t W = 2 * (size_t)WH;
+  if (o0_dev) o0 += *o0_dev;
 #pragma unroll
   for (int p = 0; p < PERL; ++p) {
 #pragma unroll

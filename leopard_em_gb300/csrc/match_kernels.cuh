@@ -194,20 +194,22 @@ __device__ inline void projection_norm_constants(const double* rs, int h, int H,
 
 // ---------------------------------------------------------------------------
 // pad_rfft: A[c][y][k] = rfft_W( normalised projection row y, zero padded )
-// for k = 0..W/2, zeros up to Wcp.  Real FFT of length W = 2*WH through a
+// for k = 0..W/2, zeros up to Wcp.  The normalisation is that of a
+// norm_h x norm_w micrograph (W may exceed norm_w when the micrograph was
+// zero padded to a supported FFT length).  Real FFT of length W = 2*WH through a
 // WH-point complex FFT (first pass pruned to the ceil(h/2) non-zero inputs).
 // ---------------------------------------------------------------------------
 template <int WH, int ROWS>
 __global__ void __launch_bounds__(ROWS* FftThreads<WH>::value)
-    pad_rfft_kernel(const float* __restrict__ proj, const double* __restrict__ rowstats, int h, int H,
-                    int Wcp, float2* __restrict__ A) {
+    pad_rfft_kernel(const float* __restrict__ proj, const double* __restrict__ rowstats, int h, int norm_h,
+                    int norm_w, int Wcp, float2* __restrict__ A) {
   constexpr int NT = FftThreads<WH>::value;
   constexpr int ZS = IdxPad16::pad(WH) + 2;
   __shared__ float2 z[ROWS][ZS];
   __shared__ float norm[2];
   const int c = blockIdx.y;
-  const int W = 2 * WH;
-  if (threadIdx.x < 32) projection_norm_constants(rowstats + (size_t)c * h * 3, h, H, W, &norm[0], &norm[1]);
+  if (threadIdx.x < 32)
+    projection_norm_constants(rowstats + (size_t)c * h * 3, h, norm_h, norm_w, &norm[0], &norm[1]);
   __syncthreads();
   const float e = norm[0], s = norm[1];
   const int g = threadIdx.x / NT, t = threadIdx.x - (threadIdx.x / NT) * NT;
@@ -243,32 +245,40 @@ __global__ void __launch_bounds__(ROWS* FftThreads<WH>::value)
 //   P = FFT_y(A_c[0..h), zero padded to HN);  X = I * conj(P), X[0,0] = 0;
 //   Y_c = IFFT_y(X)   (unscaled)
 // ---------------------------------------------------------------------------
+// Columns per colpass CTA: kColGroup, or 2 where four transforms of length HN
+// would need more than 1024 threads (HN = 5760).
 template <int HN>
-__global__ void __launch_bounds__(kColGroup* FftThreads<HN>::value, 1)
+struct ColGroupOf {
+  static constexpr int value = kColGroup * FftThreads<HN>::value <= 1024 ? kColGroup : 2;
+};
+
+template <int HN>
+__global__ void __launch_bounds__(ColGroupOf<HN>::value* FftThreads<HN>::value, 1)
     colpass_kernel(const float2* __restrict__ A, const float2* __restrict__ Ip, int h, int Wcp, int n_c,
                    int c_per_block, int c_per_image, int y_rows, float2* __restrict__ Y) {
   constexpr int NT = FftThreads<HN>::value;
+  constexpr int G = ColGroupOf<HN>::value;
   constexpr int STRIDE = IdxPad16::pad(HN) + 4;
   extern __shared__ float2 cbuf[];
-  const int kx0 = blockIdx.x * kColGroup;
+  const int kx0 = blockIdx.x * G;
   const int c_begin = blockIdx.y * c_per_block;
   const int c_end = min(n_c, c_begin + c_per_block);
   const int g = threadIdx.x / NT, t = threadIdx.x - (threadIdx.x / NT) * NT;
-  constexpr int NTH = kColGroup * NT;
+  constexpr int NTH = G * NT;
 #pragma unroll 1
   for (int c = c_begin; c < c_end; ++c) {
     const float2* a = A + (size_t)c * h * Wcp + kx0;
 #pragma unroll 1
-    for (int e = threadIdx.x; e < h * kColGroup; e += NTH) {
-      const int y = e / kColGroup, i = e % kColGroup;
+    for (int e = threadIdx.x; e < h * G; e += NTH) {
+      const int y = e / G, i = e % G;
       cbuf[i * STRIDE + IdxPad16::f(y)] = a[(size_t)y * Wcp + i];
     }
     __syncthreads();
     block_fft_pruned_outline<HN, NT, -1, IdxPad16>(cbuf + g * STRIDE, t, h);
-#pragma unroll 2
     const float2* ipc = Ip + (size_t)(c / c_per_image) * HN * Wcp;
-    for (int e = threadIdx.x; e < HN * kColGroup; e += NTH) {
-      const int y = e / kColGroup, i = e % kColGroup;
+#pragma unroll 2
+    for (int e = threadIdx.x; e < HN * G; e += NTH) {
+      const int y = e / G, i = e % G;
       const float2 I = __ldg(ipc + (size_t)y * Wcp + kx0 + i);
       const int si = i * STRIDE + IdxPad16::f(y);
       float2 X = cmulc(I, cbuf[si]);
@@ -279,8 +289,8 @@ __global__ void __launch_bounds__(kColGroup* FftThreads<HN>::value, 1)
     block_fft_outline<HN, NT, +1, IdxPad16>(cbuf + g * STRIDE, t);
     float2* yo = Y + (size_t)c * y_rows * Wcp + kx0;
 #pragma unroll 2
-    for (int e = threadIdx.x; e < y_rows * kColGroup; e += NTH) {
-      const int y = e / kColGroup, i = e % kColGroup;
+    for (int e = threadIdx.x; e < y_rows * G; e += NTH) {
+      const int y = e / G, i = e % G;
       yo[(size_t)y * Wcp + i] = cbuf[i * STRIDE + IdxPad16::f(y)];
     }
     __syncthreads();
@@ -289,7 +299,7 @@ __global__ void __launch_bounds__(kColGroup* FftThreads<HN>::value, 1)
 
 // ---------------------------------------------------------------------------
 // rowpass: row y of every correlogram in the batch: c2r of length W = 2*WH
-// (imaginary parts of DC / Nyquist ignored), scale 1/(H W), then the fused
+// (imaginary parts of DC / Nyquist ignored), scale 1/(H W) (passed in), then the fused
 // statistics update of utils.py:191-255 (max over the batch in c order with
 // strict '>', MIP update with strict '>', global index, FP64 sums).
 // ---------------------------------------------------------------------------
@@ -302,9 +312,9 @@ constexpr int row_threads(int wh, int cand = kRowThreads) {
 
 template <int WH, int NT>
 __global__ void __launch_bounds__(NT, 2)
-    rowpass_kernel(const float2* __restrict__ Y, int H, int Wcp, int n_c, int nb, int n_orient, int o0,
-                   float scale, float* __restrict__ mip, int* __restrict__ best, double* __restrict__ s1,
-                   double* __restrict__ s2) {
+    rowpass_kernel(const float2* __restrict__ Y, int y_rows, int Wcp, int n_c, int nb, int n_orient, int o0,
+                   const int* __restrict__ o0_dev, float scale, float* __restrict__ mip, int* __restrict__ best,
+                   double* __restrict__ s1, double* __restrict__ s2) {
   static_assert(NT >= FftThreads<WH>::value, "row FFT needs more threads");
   static_assert(WH % NT == 0, "row length must be a multiple of the CTA size");
   constexpr int PIX = WH / NT;
@@ -323,7 +333,7 @@ __global__ void __launch_bounds__(NT, 2)
     bss[i] = 0.f;
   }
   for (int c = 0; c < n_c; ++c) {
-    const float2* row = Y + ((size_t)c * H + y) * Wcp;
+    const float2* row = Y + ((size_t)c * y_rows + y) * Wcp;
     for (int k = t; k <= WH; k += NT) xr[k] = row[k];
     __syncthreads();
     for (int k = t; k < WH; k += NT) {
@@ -353,6 +363,7 @@ __global__ void __launch_bounds__(NT, 2)
     __syncthreads();
   }
   const size_t W = 2 * (size_t)WH;
+  if (o0_dev) o0 += *o0_dev;
 #pragma unroll
   for (int r = 0; r < PIX; ++r) {
     const size_t idx = (size_t)y * W + 2 * (size_t)(t + r * NT);

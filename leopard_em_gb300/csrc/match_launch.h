@@ -9,10 +9,10 @@ namespace lgb {
 
 // Each returns an lgb_status; LGB_ERR_UNSUPPORTED_SIZE when the FFT length is
 // not instantiated.
-// Slices for nb rotations: from Euler angles euler[o0 + b] (rotations == nullptr)
-// or from row-major 3x3 matrices rotations[9*b].
-int launch_slice(const void* vol, int d, const float* euler, int o0, int nb, const float* rotations, void* slices,
-                 cudaStream_t s);
+// Slices for nb rotations: from Euler angles euler[o0 + *o0_dev + b] (rotations
+// == nullptr; o0_dev may be null) or from row-major 3x3 matrices rotations[9*b].
+int launch_slice(const void* vol, int d, const float* euler, int o0, const int* o0_dev, int nb,
+                 const float* rotations, void* slices, cudaStream_t s);
 // Refine row pass (valid crop, z-score, per-particle packed arg-max); see refine.cu.
 int launch_refine_rowpass(int W, const void* Y, int y_rows, int Wcp, int n_cpp, int n_particles, int crop_h,
                           int crop_w, float scale, const float* corr_mean, const float* corr_std,
@@ -21,14 +21,20 @@ bool supported_refine_row(int W);
 // c = (p*n_cd + cd)*nb + b; slices [P][nb], filters [P][n_cd] (P = n_c / (n_cd*nb))
 int launch_proj_col(int h, const void* slices, const float* pf, int nb, int n_cd, int n_c, void* T, cudaStream_t s);
 int launch_proj_row(int h, const void* T, int n_c, float* proj, double* rowstats, cudaStream_t s);
-int launch_pad_rfft(int W, const float* proj, const double* rowstats, int h, int H, int Wcp, int n_c, void* A,
-                    cudaStream_t s);
+// Projections normalised for a norm_h x norm_w micrograph (utils.py:106-188),
+// rfft'd at length W (W >= norm_w: zero padding beyond the micrograph).
+int launch_pad_rfft(int W, const float* proj, const double* rowstats, int h, int norm_h, int norm_w, int Wcp,
+                    int n_c, void* A, cudaStream_t s);
 // Ip holds one padded spectrum per image; correlogram c uses image c / c_per_image.
 // Only rows y < y_rows of each inverse column transform are stored (Y is [n_c][y_rows][Wcp]).
+// waves: the correlogram range is split until the grid covers about waves x
+// the SM count (0 = 4).
 int launch_colpass(int H, const void* A, const void* Ip, int h, int Wcp, int n_c, int c_per_image, int y_rows,
-                   void* Y, cudaStream_t s);
-int launch_rowpass(int W, const void* Y, int H, int Wcp, int n_c, int nb, int n_orient, int o0, float* mip,
-                   int* best, double* s1, double* s2, cudaStream_t s);
+                   int waves, void* Y, cudaStream_t s);
+// Rows y < y_rows of the H x W correlograms (Y is [n_c][y_rows][Wcp]); global
+// index base o0 + *o0_dev (o0_dev may be null).
+int launch_rowpass(int W, const void* Y, int H, int y_rows, int Wcp, int n_c, int nb, int n_orient, int o0,
+                   const int* o0_dev, float* mip, int* best, double* s1, double* s2, cudaStream_t s);
 
 bool supported_template(int h);
 bool supported_row(int W);

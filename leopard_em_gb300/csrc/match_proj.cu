@@ -10,14 +10,16 @@ namespace lgb {
 // fftshifted slice), DC set to 0, multiplied by -1.
 // ---------------------------------------------------------------------------
 __global__ void slice_kernel(const float2* __restrict__ vol, int d, const float* __restrict__ euler, int o0,
-                             const float* __restrict__ rotations, float2* __restrict__ slices) {
+                             const int* __restrict__ o0_dev, const float* __restrict__ rotations,
+                             float2* __restrict__ slices) {
   const int b = blockIdx.y;
   __shared__ float R[9];
   if (threadIdx.x == 0) {
     if (rotations) {
       for (int i = 0; i < 9; ++i) R[i] = rotations[9 * (size_t)b + i];
     } else {
-      euler_zyz_to_rotmat(euler + 3 * (size_t)(o0 + b), R);
+      const int o = o0 + (o0_dev ? *o0_dev : 0) + b;
+      euler_zyz_to_rotmat(euler + 3 * (size_t)o, R);
     }
   }
   __syncthreads();
@@ -75,11 +77,11 @@ bool supported_template(int h) {
   }
 }
 
-int launch_slice(const void* vol, int d, const float* euler, int o0, int nb, const float* rotations, void* slices,
-                 cudaStream_t s) {
+int launch_slice(const void* vol, int d, const float* euler, int o0, const int* o0_dev, int nb,
+                 const float* rotations, void* slices, cudaStream_t s) {
   const int n_el = d * (d / 2 + 1);
   dim3 grid((n_el + 255) / 256, nb);
-  slice_kernel<<<grid, 256, 0, s>>>(static_cast<const float2*>(vol), d, euler, o0, rotations,
+  slice_kernel<<<grid, 256, 0, s>>>(static_cast<const float2*>(vol), d, euler, o0, o0_dev, rotations,
                                     static_cast<float2*>(slices));
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }

@@ -7,7 +7,8 @@
 namespace lgb {
 
 // W/2 values
-#define LGB_ROW_SIZES(X) X(24) X(32) X(40) X(64) X(128) X(144) X(256) X(288) X(512) X(1024) X(2048)
+#define LGB_ROW_SIZES(X) \
+  X(24) X(32) X(40) X(64) X(128) X(144) X(256) X(288) X(512) X(1024) X(1440) X(1536) X(1920) X(2048) X(2880)
 
 bool supported_row(int W) {
   if (W % 2) return false;
@@ -22,35 +23,38 @@ bool supported_row(int W) {
 }
 
 template <int WH>
-static int pad_rfft_t(const float* proj, const double* rowstats, int h, int H, int Wcp, int n_c, void* A,
-                      cudaStream_t s) {
+static int pad_rfft_t(const float* proj, const double* rowstats, int h, int norm_h, int norm_w, int Wcp, int n_c,
+                      void* A, cudaStream_t s) {
   constexpr int NT = FftThreads<WH>::value;
   // at least one full warp: the normalisation reduction shuffles across warp 0
   constexpr int ROWS0 = NT >= 128 ? 2 : (NT >= 32 ? 4 : 8);
-  constexpr int ROWS = ROWS0 * NT >= 32 ? ROWS0 : (32 + NT - 1) / NT;
+  constexpr int ROWS1 = ROWS0 * NT >= 32 ? ROWS0 : (32 + NT - 1) / NT;
+  // static shared memory (ROWS rows of the padded transform) stays under 40 KB
+  constexpr int ROWS = ROWS1 * (IdxPad16::pad(WH) + 2) * 8 <= 40960 ? ROWS1 : 1;
   static_assert(ROWS * NT >= 32, "pad_rfft CTA must hold a full warp");
   dim3 grid((h + ROWS - 1) / ROWS, n_c);
-  pad_rfft_kernel<WH, ROWS><<<grid, ROWS * NT, 0, s>>>(proj, rowstats, h, H, Wcp, static_cast<float2*>(A));
+  pad_rfft_kernel<WH, ROWS><<<grid, ROWS * NT, 0, s>>>(proj, rowstats, h, norm_h, norm_w, Wcp,
+                                                       static_cast<float2*>(A));
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
 template <int WH>
-static int rowpass_t(const void* Y, int H, int Wcp, int n_c, int nb, int n_orient, int o0, float* mip, int* best,
-                     double* s1, double* s2, cudaStream_t s) {
+static int rowpass_t(const void* Y, int H, int y_rows, int Wcp, int n_c, int nb, int n_orient, int o0,
+                     const int* o0_dev, float* mip, int* best, double* s1, double* s2, cudaStream_t s) {
   constexpr int NT = row_threads(WH);
   const float scale = 1.0f / ((float)H * (float)(2 * WH));
-  rowpass_kernel<WH, NT><<<H, NT, 0, s>>>(static_cast<const float2*>(Y), H, Wcp, n_c, nb, n_orient, o0, scale, mip,
-                                          best, s1, s2);
+  rowpass_kernel<WH, NT><<<y_rows, NT, 0, s>>>(static_cast<const float2*>(Y), y_rows, Wcp, n_c, nb, n_orient, o0,
+                                               o0_dev, scale, mip, best, s1, s2);
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
-int launch_pad_rfft(int W, const float* proj, const double* rowstats, int h, int H, int Wcp, int n_c, void* A,
-                    cudaStream_t s) {
-  if (W % 2) return LGB_ERR_UNSUPPORTED_SIZE;
+int launch_pad_rfft(int W, const float* proj, const double* rowstats, int h, int norm_h, int norm_w, int Wcp,
+                    int n_c, void* A, cudaStream_t s) {
+  if (W % 2 || norm_w > W || norm_w < h || norm_h < h) return LGB_ERR_UNSUPPORTED_SIZE;
   switch (W / 2) {
 #define X(n) \
   case n:    \
-    return pad_rfft_t<n>(proj, rowstats, h, H, Wcp, n_c, A, s);
+    return pad_rfft_t<n>(proj, rowstats, h, norm_h, norm_w, Wcp, n_c, A, s);
     LGB_ROW_SIZES(X)
 #undef X
     default:
@@ -59,36 +63,39 @@ int launch_pad_rfft(int W, const float* proj, const double* rowstats, int h, int
 }
 
 template <int WH, int NT, class RL>
-static int rowpass_fused_t(const void* Y, int H, int Wcp, int n_c, int nb, int n_orient, int o0, float* mip,
-                           int* best, double* s1, double* s2, cudaStream_t s) {
+static int rowpass_fused_t(const void* Y, int H, int y_rows, int Wcp, int n_c, int nb, int n_orient, int o0,
+                           const int* o0_dev, float* mip, int* best, double* s1, double* s2, cudaStream_t s) {
   using RF = RowFused<WH, NT, RL>;
   const size_t smem = RF::smem(Wcp);
   if (cudaFuncSetAttribute(rowpass_fused_kernel<WH, NT, RL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem) != cudaSuccess)
     return LGB_ERR_CUDA;
   const float scale = 1.0f / ((float)H * (float)(2 * WH));
-  rowpass_fused_kernel<WH, NT, RL><<<H, NT, smem, s>>>(static_cast<const float2*>(Y), H, Wcp, n_c, nb, n_orient, o0,
-                                                       scale, mip, best, s1, s2);
+  rowpass_fused_kernel<WH, NT, RL><<<y_rows, NT, smem, s>>>(static_cast<const float2*>(Y), y_rows, Wcp, n_c, nb,
+                                                            n_orient, o0, o0_dev, scale, mip, best, s1, s2);
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
-int launch_rowpass(int W, const void* Y, int H, int Wcp, int n_c, int nb, int n_orient, int o0, float* mip,
-                   int* best, double* s1, double* s2, cudaStream_t s) {
-  if (W % 2) return LGB_ERR_UNSUPPORTED_SIZE;
+int launch_rowpass(int W, const void* Y, int H, int y_rows, int Wcp, int n_c, int nb, int n_orient, int o0,
+                   const int* o0_dev, float* mip, int* best, double* s1, double* s2, cudaStream_t s) {
+  if (W % 2 || y_rows < 1 || y_rows > H) return LGB_ERR_INVALID_ARGUMENT;
   switch (W / 2) {
     case 2048:
-      return rowpass_fused_t<2048, 256, Radices<8, 8, 8, 4>>(Y, H, Wcp, n_c, nb, n_orient, o0, mip, best, s1, s2, s);
+      return rowpass_fused_t<2048, 256, Radices<8, 8, 8, 4>>(Y, H, y_rows, Wcp, n_c, nb, n_orient, o0, o0_dev, mip,
+                                                             best, s1, s2, s);
     case 1024:
-      return rowpass_fused_t<1024, 256, Radices<8, 8, 4, 4>>(Y, H, Wcp, n_c, nb, n_orient, o0, mip, best, s1, s2, s);
+      return rowpass_fused_t<1024, 256, Radices<8, 8, 4, 4>>(Y, H, y_rows, Wcp, n_c, nb, n_orient, o0, o0_dev, mip,
+                                                             best, s1, s2, s);
     case 256:
-      return rowpass_fused_t<256, 64, Radices<8, 8, 4>>(Y, H, Wcp, n_c, nb, n_orient, o0, mip, best, s1, s2, s);
+      return rowpass_fused_t<256, 64, Radices<8, 8, 4>>(Y, H, y_rows, Wcp, n_c, nb, n_orient, o0, o0_dev, mip, best,
+                                                        s1, s2, s);
     default:
       break;
   }
   switch (W / 2) {
 #define X(n) \
   case n:    \
-    return rowpass_t<n>(Y, H, Wcp, n_c, nb, n_orient, o0, mip, best, s1, s2, s);
+    return rowpass_t<n>(Y, H, y_rows, Wcp, n_c, nb, n_orient, o0, o0_dev, mip, best, s1, s2, s);
     LGB_ROW_SIZES(X)
 #undef X
     default:

@@ -379,11 +379,11 @@ int lgb_refine_search(const lgb_refine_problem* p, const lgb_ctf_params* ctf, co
     const int n_c = P * n_cpp;
     refine_rotations_kernel<<<(P * nb + 127) / 128, 128, 0, s>>>(euler_angles, euler_offsets, o0, nb, P, rot);
     if (cudaGetLastError() != cudaSuccess) return LGB_ERR_CUDA;
-    if ((st = launch_slice(template_dft, d, nullptr, 0, P * nb, rot, slices, s))) return st;
+    if ((st = launch_slice(template_dft, d, nullptr, 0, nullptr, P * nb, rot, slices, s))) return st;
     if ((st = launch_proj_col(d, slices, filt, nb, L.n_cd, n_c, T, s))) return st;
     if ((st = launch_proj_row(d, T, n_c, proj, rowstats, s))) return st;
-    if ((st = launch_pad_rfft(W, proj, rowstats, d, H, L.wcp, n_c, A, s))) return st;
-    if ((st = launch_colpass(H, A, ip, d, L.wcp, n_c, n_cpp, L.crop_h, Y, s))) return st;
+    if ((st = launch_pad_rfft(W, proj, rowstats, d, H, W, L.wcp, n_c, A, s))) return st;
+    if ((st = launch_colpass(H, A, ip, d, L.wcp, n_c, n_cpp, L.crop_h, 0, Y, s))) return st;
     if ((st = launch_refine_rowpass(W, Y, L.crop_h, L.wcp, n_cpp, P, L.crop_h, L.crop_w, scale, corr_mean, corr_std,
                                     key, cc, s)))
       return st;

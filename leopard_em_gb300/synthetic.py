@@ -16,7 +16,7 @@ Every configuration is built from one integer seed:
 from __future__ import annotations
 
 import math
-from dataclasses import dataclass, field
+from dataclasses import dataclass, field, replace
 
 import numpy as np
 import torch
@@ -139,15 +139,24 @@ class MatchWorkload:
     image: torch.Tensor | None = None
 
 
+def make_template(cfg: MatchConfig, device="cpu"):
+    """(template_dft on the CPU, blob centres) of ``cfg``'s Gaussian-blob volume."""
+    vol, centres = blob_volume(cfg.template_size, cfg.n_blobs, cfg.blob_sigma, cfg.blob_radius, cfg.seed,
+                               device=device)
+    template_dft = pp.volume_to_rfft_fourier_slice(vol).cpu()
+    return template_dft, centres
+
+
 def make_match_workload(cfg: MatchConfig, device="cpu", keep_image: bool = False,
-                        euler_angles: torch.Tensor | None = None) -> MatchWorkload:
-    """Build the ``core_match_template`` keyword arguments for ``cfg`` (CPU tensors)."""
+                        euler_angles: torch.Tensor | None = None, template=None) -> MatchWorkload:
+    """Build the ``core_match_template`` keyword arguments for ``cfg`` (CPU tensors).
+
+    ``template`` = (template_dft, centres) from ``make_template`` reuses one
+    volume across micrographs (its blob parameters must be ``cfg``'s)."""
     H, W = cfg.image_shape
     d = cfg.template_size
     rng = np.random.default_rng(cfg.seed + 1)
-    vol, centres = blob_volume(d, cfg.n_blobs, cfg.blob_sigma, cfg.blob_radius, cfg.seed, device=device)
-    template_dft = pp.volume_to_rfft_fourier_slice(vol).cpu()
-    del vol
+    template_dft, centres = make_template(cfg, device) if template is None else template
     if euler_angles is None:
         euler_angles = uniform_euler_grid(cfg.out_of_plane_step, cfg.in_plane_step)
     gen = torch.Generator(device="cpu").manual_seed(cfg.seed + 2)
@@ -199,6 +208,56 @@ def make_match_workload(cfg: MatchConfig, device="cpu", keep_image: bool = False
         euler_angles=euler_angles,
     )
     return MatchWorkload(cfg, kwargs, planted, image.cpu() if keep_image else None)
+
+
+# Batched form: micrographs of uneven sizes, one 256^3 template, 7 defocus
+# planes x 3 pixel sizes, grid 3.0 / 2.0 degrees (825,480 orientations).
+BATCHED_SIZES = ((2048, 2048), (3072, 2880), (3838, 3710), (4096, 4096), (5760, 4092))
+CONFIG_BATCHED = MatchConfig(
+    image_shape=(4096, 4096),
+    template_size=256,
+    n_blobs=2000,
+    blob_sigma=1.2,
+    blob_radius=100.0,
+    pixel_size=1.0,
+    n_particles=150,
+    snr=0.1,
+    defocus=10000.0,
+    defocus_offsets=(-600.0, -400.0, -200.0, 0.0, 200.0, 400.0, 600.0),
+    pixel_size_offsets=(-0.02, 0.0, 0.02),
+    out_of_plane_step=3.0,
+    in_plane_step=2.0,
+    orientation_batch=8,
+    plant_from_grid=False,
+    name="2dtm-batched-12-micrographs-256cube-3deg-2deg-7df-3px",
+)
+
+
+def batched_micrograph_configs(n_micrographs: int = 12, base: MatchConfig = CONFIG_BATCHED, seed: int = 0):
+    """Per-micrograph configurations of the batched form: sizes cycle through
+    ``BATCHED_SIZES``; 50-300 particles and SNR 0.05-0.2 drawn from the seed."""
+    rng = np.random.default_rng(seed + 17)
+    out = []
+    for i in range(n_micrographs):
+        out.append(replace(base, image_shape=BATCHED_SIZES[i % len(BATCHED_SIZES)],
+                           n_particles=int(rng.integers(50, 301)), snr=float(rng.uniform(0.05, 0.2)),
+                           seed=base.seed + 1000 * (i + 1), name=f"{base.name}/{i}"))
+    return out
+
+
+def make_batched_workload(n_micrographs: int = 12, device="cpu", base: MatchConfig = CONFIG_BATCHED,
+                          euler_angles: torch.Tensor | None = None):
+    """(template_dft, euler_angles, [per-micrograph kwargs], configs) of the batched form."""
+    template = make_template(base, device)
+    if euler_angles is None:
+        euler_angles = uniform_euler_grid(base.out_of_plane_step, base.in_plane_step)
+    mics, cfgs = [], batched_micrograph_configs(n_micrographs, base)
+    for cfg in cfgs:
+        wl = make_match_workload(cfg, device=device, euler_angles=euler_angles, template=template)
+        kw = wl.kwargs
+        mics.append({k: kw[k] for k in ("image_dft", "ctf_filters", "whitening_filter_template", "defocus_values",
+                                         "pixel_values")})
+    return template[0], euler_angles, mics, cfgs
 
 
 @dataclass

@@ -164,7 +164,7 @@ def test_argument_errors_are_raised():
     with pytest.raises(ValueError):
         core_match_template(**kw, device=torch.device("cuda:0"), mag_matrix=torch.eye(2))
     bad = dict(kw)
-    bad["image_dft"] = torch.zeros((100, 51), dtype=torch.complex64)  # 100 is not a compiled FFT length
+    bad["image_dft"] = torch.zeros((6000, 51), dtype=torch.complex64)  # no compiled grid holds 6000 rows
     with pytest.raises(ValueError):
         core_match_template(**bad, device=torch.device("cuda:0"))
     s = MatchTemplateSearch(**kw, device=torch.device("cuda:0"), orientation_batch_size=2)
