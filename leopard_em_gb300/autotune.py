@@ -1,14 +1,17 @@
 """Autotuner for the launch parameters of the whole-orientation search.
 
-Two parameters change the speed of ``lgb_match_search`` but not its results:
-the orientation batch B (correlograms per statistics update: larger batches
-amortise the image-spectrum read and the map read-modify-write over more
-correlograms, at the cost of a larger intermediate) and the column pass's
-grid split (``col_waves``: how many waves of CTAs the correlogram loop is
-split into).  ``tune_search`` times candidates on the caller's own inputs with
-CUDA events, by coordinate descent (B first at the default split, then the
-split at the best B), and caches the winner per device and search shape in a
-JSON file (``$LEOPARD_EM_GB300_TUNE_CACHE``, default
+Three choices change the speed of ``lgb_match_search`` but not its results at
+valid positions: the correlation grid (the FFT lengths; a micrograph may be
+zero padded past the smallest compiled grid to a power of two, whose
+transforms have the register-fused kernels), the orientation batch B
+(correlograms per statistics update: larger batches amortise the
+image-spectrum read and the map read-modify-write over more correlograms, at
+the cost of a larger intermediate) and the column pass's grid split
+(``col_waves``: how many waves of CTAs the correlogram loop is split into).
+``tune_search`` times candidates on the caller's own inputs with CUDA events,
+by coordinate descent (grid at B = 8, then B on the best grid, then the split),
+and caches the winner per device and search shape in a JSON file
+(``$LEOPARD_EM_GB300_TUNE_CACHE``, default
 ``~/.cache/leopard_em_gb300/autotune.json``).  The reference has no
 counterpart: its orientation batch is a user setting
 (``ComputationalConfigMatch.batch_size``).
@@ -37,6 +40,12 @@ class SearchTuning:
     col_waves: int
     graph_batches: int
     ms_per_orientation: float
+    grid_h: int = 0  # 0: the smallest compiled grid
+    grid_w: int = 0
+
+    @property
+    def grid(self):
+        return (self.grid_h, self.grid_w) if self.grid_h > 0 and self.grid_w > 0 else None
 
     @staticmethod
     def graph_batches_for(batch: int, orientations_per_graph: int = 128) -> int:
@@ -79,10 +88,10 @@ def tuning_key(device: torch.device, grid: tuple[int, int], micrograph: tuple[in
             f"/d{template_size}/C{n_pixel_sizes}/D{n_defocus}")
 
 
-def _time_candidate(make_search, batch: int, waves: int, n_probe: int, repeats: int) -> float:
-    search = make_search(batch, waves)
+def _time_candidate(make_search, cand, n_probe: int, repeats: int) -> float:
+    search = make_search(cand)
     stream = torch.cuda.current_stream(search.device)
-    search.run(0, min(n_probe, batch))  # warm-up: first launches, lazy module loading
+    search.run(0, min(n_probe, cand[1]))  # warm-up: first launches, lazy module loading
     best = float("inf")
     for _ in range(repeats):
         a = torch.cuda.Event(enable_timing=True)
@@ -98,22 +107,27 @@ def _time_candidate(make_search, batch: int, waves: int, n_probe: int, repeats: 
 
 def tune_search(image_dft, template_dft, ctf_filters, whitening_filter_template, defocus_values, pixel_values,
                 euler_angles, device, batches=DEFAULT_BATCHES, waves=DEFAULT_WAVES, n_probe: int = 48,
-                repeats: int = 2, memory_fraction: float = 0.5, use_cache: bool = True) -> SearchTuning:
-    """Pick the orientation batch and column split for this search shape.
+                repeats: int = 2, memory_fraction: float = 0.5, use_cache: bool = True,
+                tune_grid: bool = True) -> SearchTuning:
+    """Pick the grid, orientation batch and column split for this search shape.
 
     Candidates whose workspace would exceed ``memory_fraction`` of the free
     device memory are skipped.  Probes search the first ``n_probe``
-    orientations into scratch maps (the caller's maps are not touched).
+    orientations into scratch maps (the caller's maps are not touched).  With
+    ``tune_grid`` False the grid stays the smallest compiled one, which keeps
+    the reference's circular correlation in the margin of compiled sizes.
     """
-    from .backend.core_match_template import MatchTemplateSearch, _single_cuda_device, padded_grid
+    from .backend.core_match_template import MatchTemplateSearch, _single_cuda_device, grid_candidates, padded_grid
+    from ._native import MatchProblem
+    import ctypes
 
     dev = _single_cuda_device(device)
     H, wc = image_dft.shape
     W = 2 * (wc - 1)
     d = int(template_dft.shape[0])
     C, D = int(pixel_values.shape[0]), int(defocus_values.shape[0])
-    grid = padded_grid(H, W)
-    key = tuning_key(dev, grid, (H, W), d, C, D)
+    grids = grid_candidates(H, W) if tune_grid else [padded_grid(H, W)]
+    key = tuning_key(dev, grids[0], (H, W), d, C, D) + ("/grid" if tune_grid else "")
     path = cache_path()
     if use_cache:
         hit = _load_cache(path).get(key)
@@ -132,31 +146,35 @@ def tune_search(image_dft, template_dft, ctf_filters, whitening_filter_template,
         )
         free = torch.cuda.mem_get_info(dev)[0]
 
-        def make_search(batch, w):
-            return MatchTemplateSearch(**inputs, device=dev, orientation_batch_size=batch, col_waves=w)
+        def make_search(cand):
+            g, b, w = cand
+            return MatchTemplateSearch(**inputs, device=dev, orientation_batch_size=b, col_waves=w, grid=g)
 
-        def fits(batch):
-            from ._native import MatchProblem
-            import ctypes
-
-            p = MatchProblem(grid[0], grid[1], d, C, D, n_probe, batch, H, W, 0)
+        def fits(g, b):
+            p = MatchProblem(g[0], g[1], d, C, D, n_probe, b, H, W, 0)
             need = ctypes.c_size_t(0)
             if lib().lgb_match_workspace_size(ctypes.byref(p), ctypes.byref(need)) != 0:
                 return False
             return need.value <= memory_fraction * free
 
-        cands = [b for b in batches if b >= 1 and fits(b)] or [1]
-        default_waves = 4 if 4 in waves else waves[0]
         timings = {}
-        for b in cands:
-            timings[(b, default_waves)] = _time_candidate(make_search, b, default_waves, n_probe, repeats)
-        best_b = min(cands, key=lambda b: timings[(b, default_waves)])
-        for w in waves:
-            if (best_b, w) not in timings:
-                timings[(best_b, w)] = _time_candidate(make_search, best_b, w, n_probe, repeats)
-        (b, w), ms = min(timings.items(), key=lambda kv: kv[1])
-    tuning = SearchTuning(orientation_batch=b, col_waves=w, graph_batches=SearchTuning.graph_batches_for(b),
-                          ms_per_orientation=float(ms))
+
+        def time_of(cand):
+            if cand not in timings:
+                timings[cand] = _time_candidate(make_search, cand, n_probe, repeats)
+            return timings[cand]
+
+        w0 = 4 if 4 in waves else waves[0]
+        b0 = 8 if 8 in batches else batches[0]
+        grid_cands = [g for g in grids if fits(g, b0)] or grids[:1]
+        best_g = min(grid_cands, key=lambda g: time_of((g, b0, w0)))
+        cands = [b for b in batches if b >= 1 and fits(best_g, b)] or [1]
+        best_b = min(cands, key=lambda b: time_of((best_g, b, w0)))
+        best_w = min(waves, key=lambda w: time_of((best_g, best_b, w)))
+        ms = timings[(best_g, best_b, best_w)]
+    tuning = SearchTuning(orientation_batch=best_b, col_waves=best_w,
+                          graph_batches=SearchTuning.graph_batches_for(best_b), ms_per_orientation=float(ms),
+                          grid_h=best_g[0], grid_w=best_g[1])
     if use_cache:
         _store_cache(path, key, asdict(tuning))
     return tuning

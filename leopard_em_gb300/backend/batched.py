@@ -4,10 +4,11 @@ Leopard-EM searches one micrograph per ``core_match_template`` call
 (backend/core_match_template.py:146-363), and a program loops over
 micrographs on the host.  Here one call walks every micrograph in turn on one
 CUDA stream: each micrograph's search runs on its own correlation grid (the
-next compiled FFT lengths, zero padded, see ``padded_grid``), with the
-orientation batch and column split chosen by the autotuner for that grid
-(cached per shape, so micrographs of a repeated size reuse the choice), and
-the orientation batches replayed as CUDA graphs (``lgb_match_search_graph``).
+next compiled FFT lengths, or a larger compiled grid whose transforms are
+faster, zero padded), with the grid, orientation batch and column split chosen
+by the autotuner (cached per shape, so micrographs of a repeated size reuse
+the choice), and the orientation batches replayed as CUDA graphs
+(``lgb_match_search_graph``).
 The host enqueues everything without waiting; per-micrograph device times come
 from CUDA events between micrographs.
 """
@@ -72,20 +73,21 @@ def match_template_batch(micrographs, template_dft, euler_angles, device, orient
         pending = []
         for m in micrographs:
             H, wc = m["image_dft"].shape
-            grid = padded_grid(H, 2 * (wc - 1))
             if tune:
                 t = autotune.tune_search(m["image_dft"], tdft, m["ctf_filters"], m["whitening_filter_template"],
                                          m["defocus_values"], m["pixel_values"], eul, dev, use_cache=tune_cache)
             else:
                 b = int(orientation_batch_size)
                 t = autotune.SearchTuning(b, 0, autotune.SearchTuning.graph_batches_for(b), float("nan"))
+            grid = t.grid or padded_grid(H, 2 * (wc - 1))
             a = torch.cuda.Event(enable_timing=True)
             z = torch.cuda.Event(enable_timing=True)
             a.record(stream)
             search = MatchTemplateSearch(m["image_dft"], tdft, m["ctf_filters"], m["whitening_filter_template"],
                                          m["defocus_values"], m["pixel_values"], eul, dev,
                                          orientation_batch_size=t.orientation_batch,
-                                         graph_batches=t.graph_batches if use_graphs else 0, col_waves=t.col_waves)
+                                         graph_batches=t.graph_batches if use_graphs else 0, col_waves=t.col_waves,
+                                         grid=grid)
             search.run(begin, end)
             res = search.result(to_cpu=False)
             z.record(stream)

@@ -58,6 +58,22 @@ def _ptr(t: torch.Tensor) -> int:
     return t.data_ptr()
 
 
+def grid_candidates(h: int, w: int) -> list[tuple[int, int]]:
+    """Compiled grids worth timing for an h x w micrograph: per axis the
+    smallest compiled length and the smallest compiled power of two (whose
+    transforms have the fastest kernels), smallest grid first."""
+    L = lib()
+    axes = []
+    for n, axis in ((h, 0), (w, 1)):
+        c = {int(L.lgb_match_fft_size(int(n), axis))}
+        p2 = 1 << max(0, int(n) - 1).bit_length()
+        c.add(int(L.lgb_match_fft_size(p2, axis)) if L.lgb_match_fft_size(p2, axis) == p2 else 0)
+        axes.append(sorted(x for x in c if x > 0))
+    if not axes[0] or not axes[1]:
+        raise ValueError(f"no compiled FFT grid holds a {h}x{w} micrograph")
+    return sorted(((a, b) for a in axes[0] for b in axes[1]), key=lambda g: (g[0] * g[1], g))
+
+
 def padded_grid(h: int, w: int) -> tuple[int, int]:
     """Correlation grid for an h x w micrograph: the smallest compiled FFT
     lengths >= h and >= w (equal to (h, w) when both are compiled)."""
@@ -90,10 +106,14 @@ class MatchTemplateSearch:
         orientation_batch_size: int = 1,
         graph_batches: int = 0,
         col_waves: int = 0,
+        grid: tuple[int, int] | None = None,
     ):
         """``graph_batches`` > 0 replays that many orientation batches per CUDA
         graph launch (``lgb_match_search_graph``); ``col_waves`` sets the column
-        pass launch shape (0 = default).  Neither changes any result."""
+        pass launch shape (0 = default).  Neither changes any result.
+        ``grid`` = (rows, columns) searches on a larger compiled grid than the
+        smallest one that holds the micrograph (zero padding; the valid region
+        is unchanged, the margin becomes a linear correlation)."""
         self.device = _single_cuda_device(device)
         if image_dft.dim() != 2 or template_dft.dim() != 3:
             raise ValueError("image_dft must be (H, W//2+1) and template_dft (d, d, d//2+1)")
@@ -117,7 +137,9 @@ class MatchTemplateSearch:
         if graph_batches < 0 or col_waves < 0:
             raise ValueError("graph_batches and col_waves must be >= 0")
         L = lib()
-        Hp, Wp = padded_grid(H, W)
+        Hp, Wp = padded_grid(H, W) if grid is None else (int(grid[0]), int(grid[1]))
+        if Hp < H or Wp < W:
+            raise ValueError(f"grid {Hp}x{Wp} does not hold a {H}x{W} micrograph")
         self.problem = MatchProblem(
             image_h=Hp,
             image_w=Wp,

@@ -114,6 +114,18 @@ def test_padded_grid_matches_oracle_on_valid_region(H, W, d, n_o, batch):
     _assert_parity(gpu, ref, H - d + 1, W - d + 1)
 
 
+def test_larger_grid_keeps_valid_region():
+    """A compiled size searched on a larger (power-of-two) grid, as the tuner may choose."""
+    H, W, d = 288, 288, 48
+    kw = _workload(H, W, d, 16)
+    gpu = _search(kw, 8, grid=(512, 512))
+    assert tuple(gpu["_maps"]["mip"].shape) == (512, 512)
+    ref = _oracle(kw, 8)
+    _assert_parity(gpu, ref, H - d + 1, W - d + 1)
+    with pytest.raises(ValueError):
+        MatchTemplateSearch(**kw, device=DEV, grid=(256, 512))
+
+
 @pytest.mark.parametrize("H,W,n_o,batch,graph_batches", [(256, 256, 41, 4, 3), (512, 512, 64, 8, 2),
                                                           (250, 270, 20, 3, 1)])
 def test_graph_replay_is_bitwise_equal(H, W, n_o, batch, graph_batches):
@@ -137,12 +149,13 @@ def test_autotuner_picks_valid_parameters_and_caches(tmp_path, monkeypatch):
     kw = _workload(512, 512, 64, 24, n_df=2)
     t1 = autotune.tune_search(**kw, device=DEV, batches=(2, 4, 8), waves=(2, 4), n_probe=16)
     assert t1.orientation_batch in (2, 4, 8) and t1.col_waves in (2, 4) and t1.graph_batches >= 1
+    assert t1.grid == (512, 512)  # the only candidate grid of a 512^2 micrograph
     assert t1.ms_per_orientation > 0
     assert (tmp_path / "tune.json").exists()
     t2 = autotune.tune_search(**kw, device=DEV, batches=(2, 4, 8), waves=(2, 4), n_probe=16)
     assert t2 == t1  # served from the cache
     # the tuned search gives the same MIP and indices as a plain batch-1 search
-    tuned = _search(kw, t1.orientation_batch, col_waves=t1.col_waves, graph_batches=t1.graph_batches)
+    tuned = _search(kw, t1.orientation_batch, col_waves=t1.col_waves, graph_batches=t1.graph_batches, grid=t1.grid)
     plain = _search(kw, 1)
     assert torch.equal(tuned["_maps"]["mip"], plain["_maps"]["mip"])
     assert torch.equal(tuned["_maps"]["best_global_index"], plain["_maps"]["best_global_index"])
@@ -165,9 +178,10 @@ def test_batched_driver_over_uneven_micrographs(tmp_path, monkeypatch):
     results, report = match_template_batch(mics, template[0], eul, DEV, orientation_range=(0, 16))
     assert len(results) == 4 and len(report.ms) == 4 and all(ms > 0 for ms in report.ms)
     assert report.percentile(50) <= report.percentile(99)
-    for m, res in zip(mics, results):
+    for m, res, grid in zip(mics, results, report.grids):
+        # same grid as the driver chose (the tuner may pad past the smallest one)
         single = MatchTemplateSearch(**m, template_dft=template[0], euler_angles=eul, device=DEV,
-                                     orientation_batch_size=4)
+                                     orientation_batch_size=4, grid=grid)
         single.run(0, 16)
         ref = single.result(to_cpu=True)
         H, wc = m["image_dft"].shape
