@@ -238,6 +238,26 @@ int lgb_refine_search(const lgb_refine_problem* problem, const lgb_ctf_params* c
                       size_t workspace_bytes, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Split-precision tensor-core GEMM (tcgen05), the DFT building block of the  */
+/* precision form; no reference counterpart (the reference's DFTs are        */
+/* cuFFT calls inside torch.fft).                                            */
+/* ------------------------------------------------------------------------ */
+
+/* D[m][n] = sum_k A[m][k] B[n][k] with FP32 accumulation, where A = a_hi +
+ * a_lo and B = b_hi + b_lo are 16-bit (BF16, or FP16 if f16) splits of FP32
+ * matrices; terms = 3 accumulates hi*hi + lo*hi + hi*lo, terms = 1 hi*hi only.
+ * A has m_tiles*128 rows, B n_tiles*bn rows (bn = 128 or 256), both
+ * k_chunks*64 columns, in the blocked core-matrix layout: element (r, k) of a
+ * matrix cut into TR-row tiles (TR = 128 for A, bn for B) is at
+ *   (((r/TR)*k_chunks + k/64)*(TR/8) + (r%TR)/8)*512 + ((k%64)/8)*64 + (r%8)*8 + k%8.
+ * D (device, FP32, row stride ldd) receives rows < m_valid, columns < n_valid.
+ * Device pointers 16-byte aligned.  *err (device int) is set to
+ * LGB_ERR_DEVICE_TIMEOUT if a bounded device wait ran out. */
+int lgb_tc_gemm(int m_tiles, int n_tiles, int k_chunks, int bn, int f16, int terms, const void* a_hi,
+                const void* a_lo, const void* b_hi, const void* b_lo, float* d, int ldd, int m_valid, int n_valid,
+                int* err, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Refinement proposal network (no reference counterpart: Leopard-EM has no  */
 /* learned component; closest analogue core_differentiable_refine.py).       */
 /* Activations and forward weights are BF16 (device), accumulation FP32,     */
