@@ -237,6 +237,26 @@ int lgb_refine_search(const lgb_refine_problem* problem, const lgb_ctf_params* c
                       int* best_flat, int* best_offset_begin, int* best_batch_len, void* workspace,
                       size_t workspace_bytes, void* stream);
 
+/* Precision form of lgb_match_search (mode 1: BF16 hi + lo, mode 2: FP16 hi +
+ * lo operands): the inverse column DFT of the cross power and the row c2r
+ * DFT run as split-precision DFT-GEMMs on the tcgen05 tensor cores with FP32
+ * accumulation (cross_correlation.py:137-142), the statistics update
+ * (utils.py:191-255) in the second GEMM's epilogue; everything else as in
+ * lgb_match_search, same inputs, maps and index convention.  Supported when
+ * the plain search is, the grid has no zero padding, 2H and W are multiples of
+ * 128, H, W <= 1024, and C*D*B <= 32 (lgb_match_precision_supported).  The
+ * workspace (lgb_match_precision_workspace_size bytes, 256-byte aligned) must
+ * be prepared with lgb_match_prepare_image like the plain one.
+ * device_status (device int, caller-zeroed) receives LGB_ERR_DEVICE_TIMEOUT if
+ * a bounded device-side wait ran out. */
+int lgb_match_precision_supported(const lgb_match_problem* problem, int mode);
+int lgb_match_precision_workspace_size(const lgb_match_problem* problem, size_t* bytes);
+int lgb_match_search_precision(const lgb_match_problem* problem, int mode, const void* template_dft,
+                               const float* projective_filters, const float* euler_angles, int orientation_begin,
+                               int orientation_end, float* mip, int* best_index, double* corr_sum,
+                               double* corr_sq_sum, void* workspace, size_t workspace_bytes, int* device_status,
+                               void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Split-precision tensor-core GEMM (tcgen05), the DFT building block of the  */
 /* precision form; no reference counterpart (the reference's DFTs are        */

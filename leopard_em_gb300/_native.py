@@ -93,6 +93,9 @@ _SIGNATURES = {
     "lgb_refine_supported": ([ctypes.POINTER(RefineProblem)], _I),
     "lgb_refine_workspace_size": ([ctypes.POINTER(RefineProblem), ctypes.POINTER(_SZ)], _I),
     "lgb_refine_search": ([ctypes.POINTER(RefineProblem), ctypes.POINTER(CtfParams)] + [_P] * 18 + [_SZ, _P], _I),
+    "lgb_match_precision_supported": ([_PROB, _I], _I),
+    "lgb_match_precision_workspace_size": ([_PROB, ctypes.POINTER(_SZ)], _I),
+    "lgb_match_search_precision": ([_PROB, _I, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _SZ, _P, _P], _I),
     "lgb_tc_gemm": ([_I] * 6 + [_P] * 5 + [_I, _I, _I, _P, _P], _I),
     "lgb_nn_conv3x3_forward": ([_I] * 7 + [_P] * 4 + [_P], _I),
     "lgb_nn_conv3x3_backward": ([_I] * 6 + [_P] * 6 + [_P], _I),

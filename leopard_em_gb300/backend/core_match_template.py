@@ -36,6 +36,10 @@ import torch
 from .._native import MatchProblem, check, lib
 
 
+# precision modes of lgb_match_search_precision (0 = the plain FP32 search)
+PRECISION_MODES = {"fp32": 0, "bf16x3": 1, "fp16x3": 2}
+
+
 def _single_cuda_device(device) -> torch.device:
     if isinstance(device, (list, tuple)):
         if len(device) != 1:
@@ -107,13 +111,17 @@ class MatchTemplateSearch:
         graph_batches: int = 0,
         col_waves: int = 0,
         grid: tuple[int, int] | None = None,
+        precision: str = "fp32",
     ):
         """``graph_batches`` > 0 replays that many orientation batches per CUDA
         graph launch (``lgb_match_search_graph``); ``col_waves`` sets the column
         pass launch shape (0 = default).  Neither changes any result.
         ``grid`` = (rows, columns) searches on a larger compiled grid than the
         smallest one that holds the micrograph (zero padding; the valid region
-        is unchanged, the margin becomes a linear correlation)."""
+        is unchanged, the margin becomes a linear correlation).
+        ``precision`` = "bf16x3" / "fp16x3" runs the inverse DFT stages as
+        split-precision tensor-core GEMMs (``lgb_match_search_precision``);
+        "fp32" (default) is the plain FP32 search."""
         self.device = _single_cuda_device(device)
         if image_dft.dim() != 2 or template_dft.dim() != 3:
             raise ValueError("image_dft must be (H, W//2+1) and template_dft (d, d, d//2+1)")
@@ -136,6 +144,9 @@ class MatchTemplateSearch:
             raise ValueError("orientation_batch_size must be >= 1")
         if graph_batches < 0 or col_waves < 0:
             raise ValueError("graph_batches and col_waves must be >= 0")
+        if precision not in PRECISION_MODES:
+            raise ValueError(f"precision must be one of {sorted(PRECISION_MODES)}, got {precision!r}")
+        self.precision_mode = PRECISION_MODES[precision]
         L = lib()
         Hp, Wp = padded_grid(H, W) if grid is None else (int(grid[0]), int(grid[1]))
         if Hp < H or Wp < W:
@@ -153,6 +164,12 @@ class MatchTemplateSearch:
             col_waves=int(col_waves),
         )
         self.graph_batches = int(graph_batches)
+        if self.precision_mode and not L.lgb_match_precision_supported(ctypes.byref(self.problem),
+                                                                       self.precision_mode):
+            raise ValueError(
+                f"precision {precision!r} does not support this shape (image {H}x{W}, template {d}, "
+                f"{n_cs * n_df * orientation_batch_size} correlograms per batch)"
+            )
         if not L.lgb_match_supported(ctypes.byref(self.problem)):
             raise ValueError(
                 f"unsupported search shape: image {H}x{W} (grid {Hp}x{Wp}), template {d} "
@@ -182,7 +199,12 @@ class MatchTemplateSearch:
                 "lgb_match_filters",
             )
             nbytes = ctypes.c_size_t(0)
-            check(L.lgb_match_workspace_size(ctypes.byref(self.problem), ctypes.byref(nbytes)), "workspace size")
+            if self.precision_mode:
+                check(L.lgb_match_precision_workspace_size(ctypes.byref(self.problem), ctypes.byref(nbytes)),
+                      "precision workspace size")
+            else:
+                check(L.lgb_match_workspace_size(ctypes.byref(self.problem), ctypes.byref(nbytes)), "workspace size")
+            self.device_status = torch.zeros(1, dtype=torch.int32, device=dev)
             self.workspace = torch.empty(int(nbytes.value), dtype=torch.uint8, device=dev)
             self.mip = torch.empty((Hp, Wp), dtype=torch.float32, device=dev)
             self.best_index = torch.empty((Hp, Wp), dtype=torch.int32, device=dev)
@@ -224,6 +246,17 @@ class MatchTemplateSearch:
             raise ValueError(f"orientation range [{begin}, {end}) outside [0, {self.problem.n_orientations})")
         with torch.cuda.device(self.device):
             s = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+            if self.precision_mode:
+                check(
+                    lib().lgb_match_search_precision(
+                        ctypes.byref(self.problem), self.precision_mode, _ptr(self.template_dft),
+                        _ptr(self.projective_filters), _ptr(self.euler_angles), int(begin), int(end), _ptr(self.mip),
+                        _ptr(self.best_index), _ptr(self.corr_sum), _ptr(self.corr_sq_sum), _ptr(self.workspace),
+                        self.workspace.numel(), _ptr(self.device_status), s),
+                    "lgb_match_search_precision",
+                )
+                self.orientations_done += end - begin
+                return
             if self.graph_batches > 0:
                 check(
                     lib().lgb_match_search_graph(
@@ -275,6 +308,10 @@ class MatchTemplateSearch:
         H, W = self.shape
         Hp, Wp = self.grid
         dev = self.device
+        if self.precision_mode:
+            status = int(self.device_status.item())
+            if status:
+                check(status, "device-side status of the search")
         with torch.cuda.device(dev):
             s = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
             out = {k: torch.empty((Hp, Wp), dtype=torch.float32, device=dev) for k in
