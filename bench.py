@@ -61,6 +61,9 @@ def _args():
     ap.add_argument("--refine-particles", type=int, default=8)
     ap.add_argument("--no-refine", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--precision-error-orient", type=int, default=256,
+                    help="orientations of the small configuration checked against the FP64 oracle")
     ap.add_argument("--batched-micrographs", type=int, default=12)
     ap.add_argument("--batched-orient", type=int, default=48,
                     help="orientations searched per micrograph in the batched-form sample")
@@ -163,6 +166,93 @@ def _peaks():
             return json.load(f), "measured"
     except Exception:
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def precision_bench(args, dev):
+    """Precision form on the small configuration (512^2 image, 64^3 template,
+    grid 20/20 deg = 1,908 orientations): the inverse column and row DFTs as
+    split-precision tcgen05 DFT-GEMMs.  Orientations/s of the whole grid for
+    the plain FP32 kernels (B = 8 as configured, and B = 32) and the BF16x3 /
+    FP16x3 precision forms (B = 32), device-timed; MIP, argmax and z-score
+    error of each against an FP64 oracle on the first
+    ``--precision-error-orient`` orientations."""
+    from leopard_em_gb300 import synthetic as sy
+    from leopard_em_gb300._native import StageProfile
+    from leopard_em_gb300.backend import MatchTemplateSearch
+    from oracle import ref_match_template as orc
+
+    wl = sy.make_match_workload(sy.CONFIG_SMALL, device=dev)
+    kw = wl.kwargs
+    N = int(kw["euler_angles"].shape[0])
+    H, W = sy.CONFIG_SMALL.image_shape
+    d = sy.CONFIG_SMALL.template_size
+    stream = torch.cuda.current_stream(dev)
+    peaks, _ = _peaks()
+    modes = [("fp32_b8", "fp32", 8), ("fp32_b32", "fp32", 32), ("bf16x3_b32", "bf16x3", 32),
+             ("fp16x3_b32", "fp16x3", 32)]
+    out = {}
+    for label, prec, B in modes:
+        s = MatchTemplateSearch(**kw, device=dev, orientation_batch_size=B, precision=prec)
+        s.run(0, N)  # warm-up: the whole grid once
+        reps = 5
+        a = torch.cuda.Event(enable_timing=True)
+        z = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        a.record(stream)
+        for _ in range(reps):
+            s.run(0, N)
+        z.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = a.elapsed_time(z) / reps
+        with StageProfile() as prof:
+            s.run(0, N)
+            torch.cuda.synchronize(dev)
+        entry = {"orientations_per_s": N / (ms / 1e3), "ms_per_grid": ms, "orientation_batch": B,
+                 "stage_ms": {k: round(v, 4) for k, v in prof.ms.items() if prof.launches[k]}}
+        if prec != "fp32":
+            wq = -(-(W // 2 + 1) // 32) * 32
+            n_cp = 1 << (B - 1).bit_length()
+            flops = {  # useful FLOPs of the three split terms per full batch
+                "dft_col_gemm": 2.0 * (2 * H) * (B * wq) * (2 * H) * 3,
+                "dft_row_gemm": 2.0 * W * (H * n_cp) * (-(-(2 * (W // 2 + 1)) // 64) * 64) * 3,
+            }
+            tc = {}
+            for k, f in flops.items():
+                per = prof.ms[k] / max(1, prof.launches[k])
+                tc[k] = {"tflops": f / (per / 1e3) / 1e12, "per_launch_ms": per,
+                         "frac_of_bf16_peak": f / (per / 1e3) / 1e12 / peaks.get("bf16_tflops", 1900.0)}
+            entry["tensor"] = tc
+        out[label] = entry
+        del s
+    # errors against the FP64 oracle on a prefix of the grid
+    n_err = max(1, min(args.precision_error_orient, N))
+    sub = dict(kw)
+    sub["euler_angles"] = kw["euler_angles"][:n_err]
+    cpu = {k: v.cpu() for k, v in sub.items()}
+    torch.set_num_threads(os.cpu_count() or 1)
+    ref = orc.core_match_template_cpu(**cpu, orientation_batch_size=32, backend="batched", stat_dtype=torch.float64,
+                                      track_second_best=True, compute_dtype=torch.float64)
+    mip_r = ref["mip"].double()
+    scale = mip_r.abs().clamp_min(1.0)
+    sep = (mip_r - ref["second_best"].double()) > 1e-3 * scale
+    for label, prec, B in modes:
+        s = MatchTemplateSearch(**sub, device=dev, orientation_batch_size=B, precision=prec)
+        s.run()
+        res = s.result(to_cpu=True)
+        best = s.best_index.cpu().long()
+        out[label]["vs_fp64"] = {
+            "orientations": n_err,
+            "mip_max_rel_err": ((res["mip"].double() - mip_r).abs() / scale).max().item(),
+            "argmax_agreement_separated": ((best == ref["best_global_index"].long()) | ~sep).double().mean().item(),
+            "argmax_agreement_all": (best == ref["best_global_index"].long()).double().mean().item(),
+            "z_max_abs_err": (res["scaled_mip"].double() - ref["scaled_mip"].double()).abs().max().item(),
+        }
+        del s
+    base = out["fp32_b8"]["orientations_per_s"]
+    return {"workload": sy.CONFIG_SMALL.name + " (precision form)", "image": [H, W], "template": d,
+            "orientations_total": N, "runs": out,
+            "speedup_bf16x3_vs_fp32_b8": out["bf16x3_b32"]["orientations_per_s"] / base,
+            "speedup_bf16x3_vs_fp32_b32": out["bf16x3_b32"]["orientations_per_s"] / out["fp32_b32"]["orientations_per_s"]}
 
 
 def batched_bench(args, dev):
@@ -457,6 +547,9 @@ def main():
     batched = None
     if rank == 0 and world == 1 and not args.no_batched:
         batched = batched_bench(args, dev)
+    precision = None
+    if rank == 0 and world == 1 and not args.no_precision:
+        precision = precision_bench(args, dev)
 
     if rank == 0:
         line = {
@@ -473,6 +566,7 @@ def main():
             "clocks": clocks.summary(),
             "refine": refine,
             "batched": batched,
+            "precision": precision,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

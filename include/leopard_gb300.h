@@ -74,7 +74,10 @@ enum {
   LGB_STAGE_PAD_RFFT = 3, /* normalisation + zero-padded row rfft              */
   LGB_STAGE_COLPASS = 4,  /* column FFT, cross power, inverse column FFT       */
   LGB_STAGE_ROWPASS = 5,  /* row c2r + MIP / index / sum statistics            */
-  LGB_N_STAGES = 6
+  LGB_STAGE_COLFWD = 6,   /* precision form: column FFT + cross power -> operand */
+  LGB_STAGE_DFT_COL = 7,  /* precision form: inverse column DFT-GEMM (tcgen05)   */
+  LGB_STAGE_DFT_ROW = 8,  /* precision form: row c2r DFT-GEMM + statistics       */
+  LGB_N_STAGES = 9
 };
 
 /* Human-readable text of a status code (static storage). */

@@ -111,7 +111,8 @@ _SIGNATURES = {
 }
 
 
-STAGE_NAMES = ("slice", "proj_col", "proj_row", "pad_rfft", "colpass", "rowpass")
+STAGE_NAMES = ("slice", "proj_col", "proj_row", "pad_rfft", "colpass", "rowpass", "colfwd", "dft_col_gemm",
+               "dft_row_gemm")
 
 
 class StageProfile:

@@ -7,6 +7,7 @@
 #include "match_kernels.cuh"
 #include "match_launch.h"
 #include "match_layout.h"
+#include "profiler.h"
 
 namespace lgb {
 
@@ -73,21 +74,11 @@ static std::mutex g_prof_mu;
 static bool g_prof_on = false;
 static std::vector<StageEvent> g_prof_events;
 
-struct StageScope {
-  int stage;
-  cudaStream_t s;
-  cudaEvent_t a = nullptr, b = nullptr;
-  StageScope(int st, cudaStream_t str, bool on) : stage(st), s(str) {
-    if (!on) return;
-    if (cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess) cudaEventRecord(a, s);
-  }
-  ~StageScope() {
-    if (!a || !b) return;
-    cudaEventRecord(b, s);
-    std::lock_guard<std::mutex> lk(g_prof_mu);
-    g_prof_events.push_back({stage, a, b});
-  }
-};
+bool profiling_on() { return g_prof_on; }
+void profile_record(int stage, cudaEvent_t a, cudaEvent_t b) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof_events.push_back({stage, a, b});
+}
 
 static int grid_for(long long n) {
   long long g = (n + 255) / 256;
@@ -152,7 +143,7 @@ static int run_batch(const SearchArgs& a, int o0, const int* o0_dev, int nb, boo
   const int y_rows = mic_h(p);
   const int n_cd = p->n_pixel_sizes * p->n_defocus;
   const int n_c = n_cd * nb;
-  const bool prof = profile && g_prof_on;
+  const bool prof = profile && profiling_on();
   int st;
   {
     StageScope sc(LGB_STAGE_SLICE, s, prof);

@@ -34,6 +34,7 @@
 
 #include "match_launch.h"
 #include "match_layout.h"
+#include "profiler.h"
 #include "tc_gemm.cuh"
 
 namespace lgb {
@@ -162,13 +163,18 @@ __global__ void f2_kernel(int W, int kc, uint16_t* hi, uint16_t* lo) {
 // colfwd: pruned forward column FFT of the padded projection rows, cross
 // power with the image spectrum, written as the split operand B1.
 // ----------------------------------------------------------------------------
+// Eight columns per CTA: the eight operand rows (c, kx0..kx0+7) of one
+// 8-element k group form one 128-byte core matrix, written by eight
+// consecutive threads.
+constexpr int kColfwdG = 8;
+
 template <int HN, bool F16>
-__global__ void __launch_bounds__(ColGroupOf<HN>::value* FftThreads<HN>::value, 1)
+__global__ void __launch_bounds__(kColfwdG* FftThreads<HN>::value, 1)
     colfwd_kernel(const float2* __restrict__ A, const float2* __restrict__ Ip, int h, int Wcp, int wc, int wq,
                   int n_c, int c_per_block, int kc1, float xscale, uint16_t* __restrict__ b1_hi,
                   uint16_t* __restrict__ b1_lo) {
   constexpr int NT = FftThreads<HN>::value;
-  constexpr int G = ColGroupOf<HN>::value;
+  constexpr int G = kColfwdG;
   constexpr int STRIDE = IdxPad16::pad(HN) + 4;
   constexpr int NTH = G * NT;
   extern __shared__ float2 cbuf[];
@@ -181,13 +187,14 @@ __global__ void __launch_bounds__(ColGroupOf<HN>::value* FftThreads<HN>::value, 
     const float2* a = A + (size_t)c * h * Wcp + kx0;
     for (int e = threadIdx.x; e < h * G; e += NTH) {
       const int y = e / G, i = e % G;
-      cbuf[i * STRIDE + IdxPad16::f(y)] = a[(size_t)y * Wcp + i];
+      cbuf[i * STRIDE + IdxPad16::f(y)] = kx0 + i < wc ? a[(size_t)y * Wcp + i] : make_float2(0.f, 0.f);
     }
     __syncthreads();
     block_fft_pruned_outline<HN, NT, -1, IdxPad16>(cbuf + g * STRIDE, t, h);
-    // cross power, 4 rows x 1 column per item -> 8 consecutive k of row n
+    // cross power, 4 rows x 1 column per item -> 8 consecutive k of row n;
+    // the column index runs fastest (coalesced image reads, whole core matrices)
     for (int e = threadIdx.x; e < G * (HN / 4); e += NTH) {
-      const int i = e / (HN / 4), q = e - (e / (HN / 4)) * (HN / 4);
+      const int i = e % G, q = e / G;
       const int kx = kx0 + i;
       if (kx >= wc) continue;
       float v[8];
@@ -229,14 +236,16 @@ struct EpiColToRow {
     // even lane: kx offsets 0..15, odd lane 16..31; 4 groups of 4 kx = 8 k each
 #pragma unroll
     for (int gq = 0; gq < 4; ++gq) {
-      const int j0 = (ri ? 16 : 0) + 4 * gq;
-      const int kx = kxb + j0;
+      const int kx = kxb + (ri ? 16 : 0) + 4 * gq;
       if (kx >= p.wc) continue;
       float x8[8];
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
-        const float re = ri ? o[j0 + r] : v[j0 + r];
-        const float im = ri ? v[j0 + r] : o[j0 + r];
+        // compile-time indices only (the values stay in registers)
+        const float mine = ri ? v[16 + 4 * gq + r] : v[4 * gq + r];
+        const float other = ri ? o[16 + 4 * gq + r] : o[4 * gq + r];
+        const float re = ri ? other : mine;
+        const float im = ri ? mine : other;
         const bool ok = kx + r < p.wc;
         x8[2 * r] = ok ? re : 0.f;
         x8[2 * r + 1] = ok ? im : 0.f;
@@ -259,17 +268,19 @@ struct EpiRowStats {
     int H, W, n_c, n_cp, nb, n_orient, o0;
     float scale;
   };
-  static __device__ __forceinline__ void apply(int row, int col0, const float* v, const Params& p) {
-    const int x = row;
-    if (x >= p.W) return;
-    const int groups = 32 / p.n_cp;
-    for (int gi = 0; gi < groups; ++gi) {
-      const int y = (col0 + gi * p.n_cp) / p.n_cp;
+  // NCP = n_cp as a compile-time constant keeps v[] in registers
+  template <int NCP>
+  static __device__ __forceinline__ void fold(int x, int col0, const float* v, const Params& p) {
+#pragma unroll
+    for (int gi = 0; gi < 32 / NCP; ++gi) {
+      const int y = col0 / NCP + gi;
       if (y >= p.H) break;
       float bmax = -INFINITY, bs = 0.f, bss = 0.f;
       int barg = 0;
-      for (int c = 0; c < p.n_c; ++c) {
-        const float a = v[gi * p.n_cp + c] * p.scale;
+#pragma unroll
+      for (int c = 0; c < NCP; ++c) {
+        if (c >= p.n_c) break;
+        const float a = v[gi * NCP + c] * p.scale;
         if (a > bmax) {
           bmax = a;
           barg = c;
@@ -284,6 +295,17 @@ struct EpiRowStats {
       }
       p.s1[idx] += (double)bs;
       p.s2[idx] += (double)bss;
+    }
+  }
+  static __device__ __forceinline__ void apply(int row, int col0, const float* v, const Params& p) {
+    if (row >= p.W) return;
+    switch (p.n_cp) {
+      case 1: fold<1>(row, col0, v, p); break;
+      case 2: fold<2>(row, col0, v, p); break;
+      case 4: fold<4>(row, col0, v, p); break;
+      case 8: fold<8>(row, col0, v, p); break;
+      case 16: fold<16>(row, col0, v, p); break;
+      default: fold<32>(row, col0, v, p); break;
     }
   }
 };
@@ -303,7 +325,8 @@ template <int HN, bool F16>
 static int colfwd_t(const void* A, const void* Ip, int h, int Wcp, int wc, int wq, int n_c, int kc1, float xs,
                     uint16_t* hi, uint16_t* lo, cudaStream_t s) {
   constexpr int NT = FftThreads<HN>::value;
-  constexpr int G = ColGroupOf<HN>::value;
+  constexpr int G = kColfwdG;
+  static_assert(G * NT <= 1024, "colfwd CTA size");
   const size_t smem = sizeof(float2) * G * (IdxPad16::pad(HN) + 4);
   if (cudaFuncSetAttribute(colfwd_kernel<HN, F16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
@@ -311,7 +334,7 @@ static int colfwd_t(const void* A, const void* Ip, int h, int Wcp, int wc, int w
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int groups = Wcp / G;
+  const int groups = (wc + G - 1) / G;
   int split = 1;
   while (split < n_c && groups * split < 4 * sms) split *= 2;
   if (split > n_c) split = n_c;
@@ -365,19 +388,41 @@ static int precision_search(const lgb_match_problem* p, const void* template_dft
   for (int o0 = begin; o0 < end; o0 += p->orientation_batch) {
     const int nb = (end - o0) < p->orientation_batch ? (end - o0) : p->orientation_batch;
     const int n_c = n_cd * nb;
-    if ((st = launch_slice(template_dft, h, euler, o0, nullptr, nb, nullptr, slices, s))) return st;
-    if ((st = launch_proj_col(h, slices, pf, nb, n_cd, n_c, T, s))) return st;
-    if ((st = launch_proj_row(h, T, n_c, proj, rowstats, s))) return st;
-    if ((st = launch_pad_rfft(W, proj, rowstats, h, H, W, B.wcp, n_c, A, s))) return st;
-    if ((st = launch_colfwd<F16>(H, A, ip, h, B.wcp, wc, L.wq, n_c, L.kc1, xs, u16(L.b1_hi), u16(L.b1_lo), s)))
-      return st;
+    const bool prof = profiling_on();
+    {
+      StageScope sc(LGB_STAGE_SLICE, s, prof);
+      if ((st = launch_slice(template_dft, h, euler, o0, nullptr, nb, nullptr, slices, s))) return st;
+    }
+    {
+      StageScope sc(LGB_STAGE_PROJ_COL, s, prof);
+      if ((st = launch_proj_col(h, slices, pf, nb, n_cd, n_c, T, s))) return st;
+    }
+    {
+      StageScope sc(LGB_STAGE_PROJ_ROW, s, prof);
+      if ((st = launch_proj_row(h, T, n_c, proj, rowstats, s))) return st;
+    }
+    {
+      StageScope sc(LGB_STAGE_PAD_RFFT, s, prof);
+      if ((st = launch_pad_rfft(W, proj, rowstats, h, H, W, B.wcp, n_c, A, s))) return st;
+    }
+    {
+      StageScope sc(LGB_STAGE_COLFWD, s, prof);
+      if ((st = launch_colfwd<F16>(H, A, ip, h, B.wcp, wc, L.wq, n_c, L.kc1, xs, u16(L.b1_hi), u16(L.b1_lo), s)))
+        return st;
+    }
     const int n1_tiles = (n_c * L.wq + kPrecBN - 1) / kPrecBN;
-    TcGemmArgs g1{u16(L.f1_hi), u16(L.f1_lo), u16(L.b1_hi), u16(L.b1_lo), L.kc1, 3, dstatus};
-    typename EpiColToRow<F16>::Params e1{u16(L.b2_hi), u16(L.b2_lo), wc, L.wq, n_c, L.n_cp, L.kc2};
-    if ((st = launch_gemm<EpiColToRow<F16>, F16>(L.m1_tiles, n1_tiles, g1, e1, s))) return st;
-    TcGemmArgs g2{u16(L.f2_hi), u16(L.f2_lo), u16(L.b2_hi), u16(L.b2_lo), L.kc2, 3, dstatus};
-    EpiRowStats::Params e2{mip, best, s1, s2, H, W, n_c, L.n_cp, nb, p->n_orientations, o0, out_scale};
-    if ((st = launch_gemm<EpiRowStats, F16>(L.m2_tiles, L.n2_tiles, g2, e2, s))) return st;
+    {
+      StageScope sc(LGB_STAGE_DFT_COL, s, prof);
+      TcGemmArgs g1{u16(L.f1_hi), u16(L.f1_lo), u16(L.b1_hi), u16(L.b1_lo), L.kc1, 3, dstatus};
+      typename EpiColToRow<F16>::Params e1{u16(L.b2_hi), u16(L.b2_lo), wc, L.wq, n_c, L.n_cp, L.kc2};
+      if ((st = launch_gemm<EpiColToRow<F16>, F16>(L.m1_tiles, n1_tiles, g1, e1, s))) return st;
+    }
+    {
+      StageScope sc(LGB_STAGE_DFT_ROW, s, prof);
+      TcGemmArgs g2{u16(L.f2_hi), u16(L.f2_lo), u16(L.b2_hi), u16(L.b2_lo), L.kc2, 3, dstatus};
+      EpiRowStats::Params e2{mip, best, s1, s2, H, W, n_c, L.n_cp, nb, p->n_orientations, o0, out_scale};
+      if ((st = launch_gemm<EpiRowStats, F16>(L.m2_tiles, L.n2_tiles, g2, e2, s))) return st;
+    }
   }
   return LGB_OK;
 }
