@@ -15,8 +15,9 @@ the running statistics maps, exactly as one slice of a full search.
                correlogram intermediate, far larger than the 129 MB L2.
 ``e2e``        the same metric through the public drop-in
                ``core_match_template`` called with pinned host tensors: every
-               step uploads its inputs, searches its chunk, finalises and
-               copies the result maps back to the host.
+               call uploads its inputs, searches a slice of ``--e2e-orient``
+               orientations (default 1536), finalises and copies the result
+               maps back to the host.
 ``roofline``   the dominant kernel's algorithmic HBM bytes per launch over its
                mean event-timed duration, against the measured copy bandwidth.
 ``cpu_baseline`` the CPU oracle (a restatement of the reference's CPU path,
@@ -54,6 +55,8 @@ def _args():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--orient-per-step", type=int, default=96)
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-orient", type=int, default=1536,
+                    help="orientations per end-to-end call (a slice of the grid, as a caller splitting the search)")
     ap.add_argument("--cpu-sample-orient", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--config", choices=["production", "small"], default="production")
@@ -518,11 +521,17 @@ def main():
     host = {}
     for k, v in kw.items():
         host[k] = v.pin_memory() if v.device.type == "cpu" else v.cpu().pin_memory()
-    h2d = sum(v.numel() * v.element_size() for k, v in host.items() if k != "euler_angles") + chunk * 3 * 4
+    e2e_chunk = max(B, (args.e2e_orient // B) * B)
+
+    def e2e_range(step):
+        first = ((step * world + rank) * e2e_chunk) % max(1, N - e2e_chunk)
+        return first, first + e2e_chunk
+
+    h2d = sum(v.numel() * v.element_size() for k, v in host.items() if k != "euler_angles") + e2e_chunk * 3 * 4
     e2e_times = []
     d2h = 0
     for i in range(args.warmup + args.e2e_steps if args.e2e_steps > 0 else 0):
-        a, b = chunk_range(i)
+        a, b = e2e_range(i)
         kw_i = dict(host)
         kw_i["euler_angles"] = host["euler_angles"][a:b]
         torch.cuda.synchronize(dev)
@@ -532,7 +541,7 @@ def main():
         if i >= args.warmup:
             e2e_times.append(time.perf_counter() - t0)
         d2h = sum(v.numel() * v.element_size() for v in res.values() if isinstance(v, torch.Tensor))
-    e2e_val = chunk / statistics.median(e2e_times) * world if e2e_times else None
+    e2e_val = e2e_chunk / statistics.median(e2e_times) * world if e2e_times else None
 
     # --- CPU baseline (rank 0, N=1 only) ---------------------------------------
     cpu = None
@@ -566,7 +575,10 @@ def main():
                        "cross_correlations_per_s": value * n_cd,
                        "l2": "inputs larger than L2 (1.6 GB correlogram intermediate per batch)",
                        "parallelism": f"orientation-sharded x{world}"},
-            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "orientations_per_call": e2e_chunk,
+                    "timing": "wall clock per core_match_template call on pinned host tensors: upload, search, "
+                              "finalize, all maps back to the host"},
             "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": gpu_launches,
             "clocks": clocks.summary(),
             "refine": refine,
