@@ -261,6 +261,26 @@ int lgb_match_search_precision(const lgb_match_problem* problem, int mode, const
                                void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Peak picking on the z-score map (analysis/zscore_metric.py:43-84,        */
+/* analysis/utils.py:6-50).                                                  */
+/* ------------------------------------------------------------------------ */
+
+/* Scratch bytes lgb_peaks_find needs for an H x W map. */
+size_t lgb_peaks_scratch_size(int H, int W, int max_rounds);
+
+/* Candidates z > cutoff of the H x W map `zscore` (device, FP32, row-major);
+ * a candidate is picked unless a picked candidate of higher rank (larger z;
+ * equal z: smaller row-major index) lies at distance sqrtf(dy^2+dx^2) <
+ * radius -- the reference's greedy walk in descending order.  Writes the flat
+ * indices of the picked peaks (unordered, device int[max_peaks]) and their
+ * number (host int, may exceed max_peaks: then only max_peaks were written),
+ * and the rounds used (host int).  Synchronises `stream`.  Returns
+ * LGB_ERR_DEVICE_TIMEOUT if the candidates did not settle in max_rounds. */
+int lgb_peaks_find(int H, int W, const float* zscore, float cutoff, float radius, int max_rounds, void* scratch,
+                   size_t scratch_bytes, int max_peaks, int* peak_index, int* n_peaks, int* rounds_used,
+                   void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Split-precision tensor-core GEMM (tcgen05), the DFT building block of the  */
 /* precision form; no reference counterpart (the reference's DFTs are        */
 /* cuFFT calls inside torch.fft).                                            */

@@ -215,18 +215,34 @@ class MatchTemplateResult:
                      "orientation_theta", "orientation_phi", "relative_defocus"):
             setattr(self, name, getattr(self, name)[sl])
 
-    def locate_peaks(self, z_score_cutoff: float = 7.0, min_distance: int = 10):
-        """(y, x) of local maxima of scaled_mip above the cutoff, greedily
-        suppressed within min_distance (the zscore-metric peak picking)."""
-        z = self.scaled_mip
-        cand = torch.nonzero(z > z_score_cutoff)
-        order = torch.argsort(z[cand[:, 0], cand[:, 1]], descending=True)
-        taken = []
-        for i in order.tolist():
-            y, x = cand[i].tolist()
-            if all((y - a) ** 2 + (x - b) ** 2 >= min_distance**2 for a, b in taken):
-                taken.append((y, x))
-        return torch.tensor(taken, dtype=torch.long).reshape(-1, 2)
+    match_template_peaks: Optional["MatchTemplatePeaks"] = None
+
+    def locate_peaks(self, **kwargs) -> "MatchTemplatePeaks":
+        """Peak positions and per-peak statistics from the held maps
+        (match_template_result.py:252-288), with the z-score peak picking on the
+        device (``peaks.extract_peaks_and_statistics_zscore``; keyword
+        arguments: false_positives, z_score_cutoff, mask_radius, device)."""
+        from .peaks import extract_peaks_and_statistics_zscore
+
+        self.match_template_peaks = extract_peaks_and_statistics_zscore(
+            mip=self.mip,
+            scaled_mip=self.scaled_mip,
+            best_psi=self.orientation_psi,
+            best_theta=self.orientation_theta,
+            best_phi=self.orientation_phi,
+            best_defocus=self.relative_defocus,
+            correlation_average=self.correlation_average,
+            correlation_variance=self.correlation_variance,
+            total_correlation_positions=self.total_projections,
+            **kwargs,
+        )
+        return self.match_template_peaks
+
+    def peaks_to_dict(self) -> dict:
+        """The located peaks as a dictionary (match_template_result.py:290-295)."""
+        if self.match_template_peaks is None:
+            self.locate_peaks()
+        return self.match_template_peaks._asdict()
 
 
 @dataclass

@@ -28,6 +28,12 @@ torch_fourier_filter replaced by the oracle's restatements
 search_utils.py, the cross-correlation, z-score, strict-'>' batch update and
 index decode -- the reference's own code.
 
+``tests/golden/peaks_small.npz`` (``--peaks``): z-score peak picking by the
+reference's ``analysis/zscore_metric.py`` (find_peaks_from_zscore,
+gaussian_noise_zscore_cutoff) and ``analysis/utils.py``
+(filter_peaks_by_distance); ``pandas`` (imported by the package's
+match_template_peaks.py, unused here) is a stand-in module.
+
 The files are small and committed; this script is not needed at test time.
 """
 
@@ -169,6 +175,52 @@ def _run_search(cc_mod, ut_mod, pr_mod, inp, batch):
     )
 
 
+def _peak_maps():
+    """Seeded z maps: N(0,1) noise plus Gaussian bumps (no exact ties)."""
+    g = torch.Generator().manual_seed(21)
+    maps = {}
+    for name, (H, W, n_bumps, amp) in {"p1": (64, 80, 6, 10.0), "p2": (96, 96, 25, 7.0), "p3": (40, 40, 0, 0.0)}.items():
+        z = torch.randn(H, W, generator=g)
+        yy, xx = torch.meshgrid(torch.arange(H, dtype=torch.float32), torch.arange(W, dtype=torch.float32),
+                                indexing="ij")
+        for _ in range(n_bumps):
+            cy, cx = (torch.rand(2, generator=g) * torch.tensor([H - 1.0, W - 1.0])).tolist()
+            sig = 1.0 + 2.0 * torch.rand(1, generator=g).item()
+            z += amp * torch.rand(1, generator=g).item() * torch.exp(-((yy - cy) ** 2 + (xx - cx) ** 2) / (2 * sig**2))
+        maps[name] = z
+    return maps
+
+
+def main_peaks(ref_root):
+    pd = types.ModuleType("pandas")
+    pd.DataFrame = dict  # only named in an annotation
+    sys.modules.setdefault("pandas", pd)
+    pkg = types.ModuleType("leopard_em_ref_analysis")
+    pkg.__path__ = [os.path.join(ref_root, "src/leopard_em/analysis")]
+    sys.modules["leopard_em_ref_analysis"] = pkg
+    mods = {}
+    for sub in ("match_template_peaks", "utils", "zscore_metric"):
+        path = os.path.join(ref_root, "src/leopard_em/analysis", sub + ".py")
+        spec = importlib.util.spec_from_file_location(f"leopard_em_ref_analysis.{sub}", path)
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[f"leopard_em_ref_analysis.{sub}"] = mod
+        spec.loader.exec_module(mod)
+        mods[sub] = mod
+    zm = mods["zscore_metric"]
+    out = {}
+    for name, z in _peak_maps().items():
+        for cutoff, radius in ((3.0, 5.0), (2.0, 2.5), (4.0, 10.0)):
+            py, px = zm.find_peaks_from_zscore(z, cutoff, radius)
+            key = f"{name}/c{cutoff}/r{radius}"
+            out[f"{key}/pos_y"] = py.numpy()
+            out[f"{key}/pos_x"] = px.numpy()
+        out[f"{name}/z"] = z.numpy()
+    n_ccg = np.array([10**6, 10**9, 4096 * 4096 * 1584000 * 3], dtype=np.float64)
+    out["cutoff/num_ccg"] = n_ccg
+    out["cutoff/value"] = np.array([zm.gaussian_noise_zscore_cutoff(int(n), fp) for n in n_ccg for fp in (1.0, 0.5)])
+    np.savez_compressed(os.path.join(HERE, "peaks_small.npz"), **out)
+
+
 def main(ref_root):
     os.environ["LEOPARDEM_DISABLE_TORCH_COMPILATION"] = "1"
     _install_stubs()
@@ -285,6 +337,10 @@ def _refine_golden(ref_root):
     np.savez_compressed(path, **out)
     print("wrote", path, os.path.getsize(path), "bytes")
 
+
+if __name__ == "__main__" and "--peaks" in sys.argv:
+    main_peaks([a for a in sys.argv[1:] if a != "--peaks"][0])
+    sys.exit(0)
 
 if __name__ == "__main__":
     main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -62,6 +62,11 @@ def test_match_manager_finds_planted_particle():
     assert abs(py - y0) <= 1 and abs(px - x0) <= 1
     assert (float(r.orientation_phi[y0, x0]), float(r.orientation_theta[y0, x0]),
             float(r.orientation_psi[y0, x0])) == pytest.approx(eul)
+    # peak picking on the device at a cutoff just under the particle's z
+    peaks = r.locate_peaks(z_score_cutoff=float(r.scaled_mip[y0, x0]) - 1e-3, mask_radius=5.0)
+    assert (int(peaks.pos_y[0]), int(peaks.pos_x[0])) == (y0, x0)
+    assert float(peaks.phi[0]) == pytest.approx(eul[0]) and peaks.total_correlations == r.total_projections
+    assert set(r.peaks_to_dict()) >= {"pos_y", "pos_x", "mip", "scaled_mip", "psi", "relative_defocus"}
 
 
 @pytest.mark.gpu
