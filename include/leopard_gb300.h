@@ -260,6 +260,20 @@ int lgb_match_search_precision(const lgb_match_problem* problem, int mode, const
                                double* corr_sq_sum, void* workspace, size_t workspace_bytes, int* device_status,
                                void* stream);
 
+/* Cross-correlation of a particle stack with one projection per particle
+ * (core_refine_template.py:771-895, cross_correlate_particle_stack).  Device
+ * inputs: particle_dft complex64 [P][H][W/2+1] (filtered, un-shifted rfft2 of
+ * the particles); template_dft complex64 [d][d][d/2+1] (fftshifted);
+ * rotations [P][3][3] row-major; projective_filters [P][d][d/2+1].  Output
+ * out [P][H-d+1][W-d+1] (mode 0, "valid") or [P][H][W] (mode 1, "same").
+ * Particles are processed `group` at a time in a workspace of
+ * lgb_xcorr_stack_workspace_size(group, ...) bytes. */
+int lgb_xcorr_stack_supported(int H, int W, int d);
+int lgb_xcorr_stack_workspace_size(int group, int H, int W, int d, int mode, size_t* bytes);
+int lgb_xcorr_stack(int n_particles, int group, int H, int W, int d, int mode, const void* particle_dft,
+                    const void* template_dft, const float* rotations, const float* projective_filters, float* out,
+                    void* workspace, size_t workspace_bytes, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Peak picking on the z-score map (analysis/zscore_metric.py:43-84,        */
 /* analysis/utils.py:6-50).                                                  */

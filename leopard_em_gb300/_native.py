@@ -96,6 +96,9 @@ _SIGNATURES = {
     "lgb_match_precision_supported": ([_PROB, _I], _I),
     "lgb_match_precision_workspace_size": ([_PROB, ctypes.POINTER(_SZ)], _I),
     "lgb_match_search_precision": ([_PROB, _I, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _SZ, _P, _P], _I),
+    "lgb_xcorr_stack_supported": ([_I, _I, _I], _I),
+    "lgb_xcorr_stack_workspace_size": ([_I, _I, _I, _I, _I, ctypes.POINTER(_SZ)], _I),
+    "lgb_xcorr_stack": ([_I] * 6 + [_P] * 6 + [_SZ, _P], _I),
     "lgb_peaks_scratch_size": ([_I, _I, _I], _SZ),
     "lgb_peaks_find": ([_I, _I, _P, ctypes.c_float, ctypes.c_float, _I, _P, _SZ, _I, _P,
                         ctypes.POINTER(_I), ctypes.POINTER(_I), _P], _I),

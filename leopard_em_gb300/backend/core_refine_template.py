@@ -183,3 +183,51 @@ def decode_refine_results(raw, stack_shape, d, euler_angles, euler_angle_offsets
         "refined_pos_x": x - (W - d + 1) // 2,
         "angle_idx": angle_idx,
     }
+
+
+def cross_correlate_particle_stack(
+    particle_stack_dft: torch.Tensor,
+    template_dft: torch.Tensor,
+    rotation_matrices: torch.Tensor,
+    projective_filters: torch.Tensor,
+    mode: str = "valid",
+    batch_size: int = 1024,
+    mag_matrix: torch.Tensor | None = None,
+    device=None,
+) -> torch.Tensor:
+    """Cross-correlate each particle with the template projected at its own
+    rotation (core_refine_template.py:771-895): returns (N, H-h+1, W-w+1)
+    for mode "valid", (N, H, W) for "same", on the particles' device (the
+    work runs on ``device`` or, for CPU inputs, the current CUDA device)."""
+    if mag_matrix is not None:
+        raise ValueError("anisotropic magnification (mag_matrix) is not supported by leopard_em_gb300")
+    if mode not in ("valid", "same"):
+        raise ValueError(f"Invalid mode: {mode}. Must be 'valid' or 'same'.")
+    N, H, wc = particle_stack_dft.shape
+    W = 2 * (wc - 1)
+    d = int(template_dft.shape[0])
+    if tuple(template_dft.shape) != (d, d, d // 2 + 1):
+        raise ValueError("template_dft must be (d, d, d//2+1)")
+    if tuple(rotation_matrices.shape) != (N, 3, 3) or tuple(projective_filters.shape) != (N, d, d // 2 + 1):
+        raise ValueError("rotation_matrices must be (N, 3, 3) and projective_filters (N, d, d//2+1)")
+    dev = _device(device if device is not None else
+                  (particle_stack_dft.device if particle_stack_dft.is_cuda else "cuda"))
+    L = lib()
+    if not L.lgb_xcorr_stack_supported(H, W, d):
+        raise ValueError(f"unsupported shape: particles {H}x{W}, template {d}")
+    group = max(1, min(N, N if batch_size == -1 else int(batch_size)))
+    m = 0 if mode == "valid" else 1
+    out_shape = (N, H - d + 1, W - d + 1) if m == 0 else (N, H, W)
+    with torch.cuda.device(dev):
+        s = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        need = ctypes.c_size_t(0)
+        check(L.lgb_xcorr_stack_workspace_size(group, H, W, d, m, ctypes.byref(need)), "xcorr workspace")
+        ws = torch.empty(int(need.value), dtype=torch.uint8, device=dev)
+        ps = particle_stack_dft.to(dev, torch.complex64).contiguous()
+        tdft = template_dft.to(dev, torch.complex64).contiguous()
+        rot = rotation_matrices.to(dev, torch.float32).contiguous()
+        pf = projective_filters.to(dev, torch.float32).contiguous()
+        out = torch.empty(out_shape, dtype=torch.float32, device=dev)
+        check(L.lgb_xcorr_stack(N, group, H, W, d, m, ps.data_ptr(), tdft.data_ptr(), rot.data_ptr(), pf.data_ptr(),
+                                out.data_ptr(), ws.data_ptr(), ws.numel(), s), "lgb_xcorr_stack")
+    return out.to(particle_stack_dft.device)

@@ -178,3 +178,29 @@ def core_refine_template_cpu(particle_stack_dft, template_dft, euler_angles, eul
         "refined_pos_x": pos_x,
         "angle_idx": torch.tensor([s["angle_idx"] for s in stats]),
     }
+
+
+def cross_correlate_particle_stack_cpu(particle_stack_dft, template_dft, rotation_matrices, projective_filters,
+                                       mode="valid"):
+    """core_refine_template.py:771-895 (no mag_matrix): per particle the slice
+    at its rotation, ifftshift rows, DC 0, contrast flip, x filter, irfft2,
+    ifftshift, normalisation for the particle size, padded rfft, particle *
+    conj(projection) (no DC zeroing), irfft2, crop (utils/cross_correlation.py:8-40)."""
+    N, H, wc = particle_stack_dft.shape
+    W = 2 * (wc - 1)
+    d = template_dft.shape[0]
+    fs = mt.extract_central_slices_rfft_3d(template_dft, rotation_matrices)
+    fs = torch.fft.ifftshift(fs, dim=(-2,))
+    fs[..., 0, 0] = 0 + 0j
+    fs = fs * -1
+    fs = fs * projective_filters
+    proj = torch.fft.irfftn(fs, dim=(-2, -1))
+    proj = torch.fft.ifftshift(proj, dim=(-2, -1))
+    proj = mt.normalize_template_projection(proj, (d, d), (H, W))
+    pdft = torch.fft.rfftn(proj, dim=(-2, -1), s=(H, W))
+    cc = torch.fft.irfftn(particle_stack_dft * pdft.conj(), dim=(-2, -1))
+    if mode == "valid":
+        cc = cc[:, : H - d + 1, : W - d + 1]
+    elif mode != "same":
+        raise ValueError(mode)
+    return cc

@@ -34,6 +34,10 @@ gaussian_noise_zscore_cutoff) and ``analysis/utils.py``
 (filter_peaks_by_distance); ``pandas`` (imported by the package's
 match_template_peaks.py, unused here) is a stand-in module.
 
+``tests/golden/xcorr_small.npz`` (``--xcorr``): the reference's
+``cross_correlate_particle_stack`` (backend/core_refine_template.py:771-895)
+on small stacks, both modes, with the stand-ins above for the slice extraction.
+
 The files are small and committed; this script is not needed at test time.
 """
 
@@ -221,6 +225,42 @@ def main_peaks(ref_root):
     np.savez_compressed(os.path.join(HERE, "peaks_small.npz"), **out)
 
 
+def main_xcorr(ref_root):
+    """cross_correlate_particle_stack (core_refine_template.py:771-895) from the
+    reference's own code -> xcorr_small.npz (particles with a non-zero DC)."""
+    os.environ["LEOPARDEM_DISABLE_TORCH_COMPILATION"] = "1"
+    _install_stubs()
+    ut = _load(ref_root, "backend/utils.py", "leopard_em_ref_utils")
+    sys.modules["leopard_em.backend.utils"] = ut
+    sys.modules.setdefault("leopard_em", types.ModuleType("leopard_em"))
+    sys.modules.setdefault("leopard_em.backend", types.ModuleType("leopard_em.backend"))
+    _load(ref_root, "backend/cross_correlation.py", "leopard_em_ref_cc")
+    for name in ("leopard_em.utils",):
+        sys.modules.setdefault(name, types.ModuleType(name))
+    _load(ref_root, "utils/search_utils.py", "leopard_em.utils.search_utils")
+    _load(ref_root, "utils/cross_correlation.py", "leopard_em.utils.cross_correlation")
+    _load(ref_root, "utils/ctf_utils.py", "leopard_em.utils.ctf_utils")
+    _load(ref_root, "backend/distributed.py", "leopard_em.backend.distributed")
+    sys.modules["leopard_em.backend.cross_correlation"] = sys.modules["leopard_em_ref_cc"]
+    rt = _load(ref_root, "backend/core_refine_template.py", "leopard_em_ref_refine")
+    g = torch.Generator().manual_seed(41)
+    out = {}
+    for name, (n_p, H, d) in {"x1": (3, 64, 32), "x2": (2, 128, 64)}.items():
+        inp = _make_inputs(41 + H, H, H, d, 1, 1, 1)
+        stack = torch.fft.rfftn(torch.randn(n_p, H, H, generator=g) + 0.3, dim=(-2, -1)).to(torch.complex64)
+        euler = (torch.rand(n_p, 3, generator=g) * torch.tensor([360.0, 180.0, 360.0])).to(torch.float32)
+        rot = sys.modules["roma"].euler_to_rotmat("ZYZ", euler, degrees=True)
+        pf = (torch.rand(n_p, d, d // 2 + 1, generator=g) + 0.5).to(torch.float32)
+        for mode in ("valid", "same"):
+            cc = rt.cross_correlate_particle_stack(stack, inp["template_dft"], rot, pf, mode=mode, batch_size=2)
+            out[f"{name}/{mode}"] = cc.numpy()
+        out[f"{name}/stack"] = stack.numpy()
+        out[f"{name}/template_dft"] = inp["template_dft"].numpy()
+        out[f"{name}/rot"] = rot.numpy()
+        out[f"{name}/filters"] = pf.numpy()
+    np.savez_compressed(os.path.join(HERE, "xcorr_small.npz"), **out)
+
+
 def main(ref_root):
     os.environ["LEOPARDEM_DISABLE_TORCH_COMPILATION"] = "1"
     _install_stubs()
@@ -337,6 +377,10 @@ def _refine_golden(ref_root):
     np.savez_compressed(path, **out)
     print("wrote", path, os.path.getsize(path), "bytes")
 
+
+if __name__ == "__main__" and "--xcorr" in sys.argv:
+    main_xcorr([a for a in sys.argv[1:] if a != "--xcorr"][0])
+    sys.exit(0)
 
 if __name__ == "__main__" and "--peaks" in sys.argv:
     main_peaks([a for a in sys.argv[1:] if a != "--peaks"][0])
