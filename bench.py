@@ -59,7 +59,8 @@ def _args():
                     help="orientations per end-to-end call (a slice of the grid, as a caller splitting the search)")
     ap.add_argument("--cpu-sample-orient", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--config", choices=["production", "small"], default="production")
+    ap.add_argument("--config", choices=["production", "small", "refbench"], default="production",
+                    help="refbench: the reference's published benchmark shape (4096^2, 512^3, 11 defocus)")
     ap.add_argument("--batch", type=int, default=0, help="orientation batch (0: the configuration's)")
     ap.add_argument("--refine-particles", type=int, default=8)
     ap.add_argument("--no-refine", action="store_true")
@@ -147,8 +148,33 @@ class ClockSampler:
 def _workload(cfg_name, device):
     from leopard_em_gb300 import synthetic as sy
 
-    cfg = sy.CONFIG_PRODUCTION if cfg_name == "production" else sy.CONFIG_SMALL
+    cfg = {"production": sy.CONFIG_PRODUCTION, "small": sy.CONFIG_SMALL, "refbench": sy.CONFIG_REFBENCH}[cfg_name]
     return sy.make_match_workload(cfg, device=device)
+
+
+def _fp32_peak(dev):
+    """Non-tensor FP32 peak (TFLOP/s) from the library's FMA probe, best of 3."""
+    import ctypes
+
+    from leopard_em_gb300._native import check, lib
+
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    blocks, iters = sms * 8, 20000
+    out = torch.zeros(1, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    s = ctypes.c_void_p(stream.cuda_stream)
+    flops = blocks * 256 * 8 * 16 * 2.0 * iters
+    best = 0.0
+    for i in range(4):
+        a = torch.cuda.Event(enable_timing=True)
+        z = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        check(lib().lgb_fp32_fma_probe(blocks, iters, out.data_ptr(), s), "lgb_fp32_fma_probe")
+        z.record(stream)
+        z.synchronize()
+        if i:
+            best = max(best, flops / (a.elapsed_time(z) / 1e3) / 1e12)
+    return best
 
 
 def _cpu_oracle_rate(kwargs, n_orient, batch, threads, start=0):
@@ -499,6 +525,7 @@ def main():
         "pad_rfft": n_c * d * 2.5 * W * math.log2(W),
     }
     stage_ms, launches = prof.ms, prof.launches
+    fp32_peak = _fp32_peak(dev)
     top = max(stage_ms, key=stage_ms.get)
     peaks, peak_kind = _peaks()
     per_launch_ms = stage_ms[top] / max(1, launches[top])
@@ -513,6 +540,7 @@ def main():
         "peak_source": peak_kind,
         "per_launch_ms": per_launch_ms,
         "fp32_tflops_achieved": (alg_flops[top] / (per_launch_ms / 1e3) / 1e12) if top in alg_flops else None,
+        "fp32_peak_tflops_measured": fp32_peak,
         "stage_share": {k: v / max(1e-9, sum(stage_ms.values())) for k, v in stage_ms.items()},
     }
     gpu_launches = int(sum(launches.values()))
@@ -542,6 +570,25 @@ def main():
             e2e_times.append(time.perf_counter() - t0)
         d2h = sum(v.numel() * v.element_size() for v in res.values() if isinstance(v, torch.Tensor))
     e2e_val = e2e_chunk / statistics.median(e2e_times) * world if e2e_times else None
+    # the reference benchmark's two-run model T = N / r + k (benchmark_match_template.py:84-123):
+    # calls of N/2 and N orientations give the rate r without the per-call set-up k
+    two_run = None
+    if e2e_times:
+        half = max(B, (e2e_chunk // 2 // B) * B)
+        t_half = []
+        for i in range(max(2, args.e2e_steps)):
+            a, _ = e2e_range(i)
+            kw_i = dict(host)
+            kw_i["euler_angles"] = host["euler_angles"][a:a + half]
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            core_match_template(**kw_i, device=dev, orientation_batch_size=B)
+            torch.cuda.synchronize(dev)
+            t_half.append(time.perf_counter() - t0)
+        t1, t2 = statistics.median(t_half), statistics.median(e2e_times)
+        if t2 > t1:
+            r = (e2e_chunk - half) / (t2 - t1)
+            two_run = {"rate": r * world, "setup_s": t1 - half / r, "n1": half, "n2": e2e_chunk}
 
     # --- CPU baseline (rank 0, N=1 only) ---------------------------------------
     cpu = None
@@ -576,7 +623,7 @@ def main():
                        "l2": "inputs larger than L2 (1.6 GB correlogram intermediate per batch)",
                        "parallelism": f"orientation-sharded x{world}"},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                    "orientations_per_call": e2e_chunk,
+                    "orientations_per_call": e2e_chunk, "two_run_model": two_run,
                     "timing": "wall clock per core_match_template call on pinned host tensors: upload, search, "
                               "finalize, all maps back to the host"},
             "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": gpu_launches,

@@ -86,6 +86,12 @@ const char* lgb_status_string(int status);
 /* Library version, major*10000 + minor*100 + patch. */
 int lgb_version(void);
 
+/* FP32 FMA throughput probe (measurement only): `blocks` CTAs of 256 threads,
+ * each thread running 8 independent chains of iters*16 FMAs (2 FLOPs each);
+ * time it with events to get the non-tensor FP32 peak.  `out` (device float)
+ * is only written if a chain sums to a sentinel (never in practice). */
+int lgb_fp32_fma_probe(int blocks, int iters, float* out, void* stream);
+
 /* Stage profiler (no reference counterpart; measurement only).  Between
  * lgb_profile_begin and lgb_profile_end every stage launch made by
  * lgb_match_search on any stream is bracketed by CUDA events on that stream.
@@ -153,6 +159,26 @@ int lgb_match_search_graph(const lgb_match_problem* problem, const void* templat
                            int orientation_end, int batches_per_graph, float* mip, int* best_index,
                            double* corr_sum, double* corr_sq_sum, void* workspace, size_t workspace_bytes,
                            void* stream);
+
+/* Plan form of the same search: an opaque handle owning the workspace, the
+ * projective filters and the four maps (device memory of the device current
+ * at creation).  create/destroy allocate and free (synchronously); the others
+ * are asynchronous on `stream`.  set_image (re)initialises the maps;
+ * finalize divides by the orientations searched since then x D x C.
+ * Replaces the per-device worker state of _core_match_template_single_gpu
+ * (core_match_template.py:369-562). */
+typedef struct lgb_match_plan lgb_match_plan;
+lgb_match_plan* lgb_match_plan_create(const lgb_match_problem* problem, int* status);
+void lgb_match_plan_destroy(lgb_match_plan* plan);
+int lgb_match_plan_set_filters(lgb_match_plan* plan, const float* ctf_filters, const float* whitening, void* stream);
+int lgb_match_plan_set_image(lgb_match_plan* plan, const void* image_dft, void* stream);
+int lgb_match_plan_search(lgb_match_plan* plan, const void* template_dft, const float* euler_angles,
+                          int orientation_begin, int orientation_end, void* stream);
+int lgb_match_plan_maps(lgb_match_plan* plan, float** mip, int** best_index, double** corr_sum,
+                        double** corr_sq_sum);
+int lgb_match_plan_finalize(lgb_match_plan* plan, const float* euler_angles, const float* defocus_values,
+                            float* scaled_mip, float* best_phi, float* best_theta, float* best_psi,
+                            float* best_defocus, float* corr_mean, float* corr_std, void* stream);
 
 /* lgb_match_search without any device allocation: no reference counterpart
  * (the reference always allocates through PyTorch).  For callers that cannot

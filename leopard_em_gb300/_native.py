@@ -79,6 +79,7 @@ _SIGNATURES = {
     "lgb_status_string": ([_I], ctypes.c_char_p),
     "lgb_version": ([], _I),
     "lgb_profile_begin": ([], _I),
+    "lgb_fp32_fma_probe": ([_I, _I, _P, _P], _I),
     "lgb_profile_end": ([ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_LL), _I], _I),
     "lgb_match_supported": ([_PROB], _I),
     "lgb_match_workspace_size": ([_PROB, ctypes.POINTER(_SZ)], _I),
@@ -88,6 +89,13 @@ _SIGNATURES = {
     "lgb_match_search": ([_PROB, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _SZ, _P], _I),
     "lgb_match_fft_size": ([_I, _I], _I),
     "lgb_match_search_graph": ([_PROB, _P, _P, _P, _I, _I, _I, _P, _P, _P, _P, _P, _SZ, _P], _I),
+    "lgb_match_plan_create": ([_PROB, ctypes.POINTER(_I)], _P),
+    "lgb_match_plan_destroy": ([_P], None),
+    "lgb_match_plan_set_filters": ([_P, _P, _P, _P], _I),
+    "lgb_match_plan_set_image": ([_P, _P, _P], _I),
+    "lgb_match_plan_search": ([_P, _P, _P, _I, _I, _P], _I),
+    "lgb_match_plan_maps": ([_P] + [ctypes.POINTER(_P)] * 4, _I),
+    "lgb_match_plan_finalize": ([_P] + [_P] * 9 + [_P], _I),
     "lgb_static_scratch_capacity": ([], _SZ),
     "lgb_match_search_static_scratch": ([_PROB, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P], _I),
     "lgb_refine_supported": ([ctypes.POINTER(RefineProblem)], _I),

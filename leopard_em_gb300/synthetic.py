@@ -131,6 +131,27 @@ CONFIG_PRODUCTION = MatchConfig(
 )
 
 
+# The shape of the reference's published benchmark (4096^2 micrograph, 512^3
+# template, 11 defocus planes), for a like-for-like correlograms/s figure.
+CONFIG_REFBENCH = MatchConfig(
+    image_shape=(4096, 4096),
+    template_size=512,
+    n_blobs=6000,
+    blob_sigma=1.2,
+    blob_radius=200.0,
+    pixel_size=1.06,
+    n_particles=100,
+    snr=0.1,
+    defocus=10000.0,
+    defocus_offsets=tuple(float(x) for x in range(-500, 501, 100)),
+    out_of_plane_step=2.5,
+    in_plane_step=1.5,
+    orientation_batch=8,
+    plant_from_grid=False,
+    name="2dtm-4096sq-512cube-2.5deg-1.5deg-11df",
+)
+
+
 @dataclass
 class MatchWorkload:
     config: MatchConfig
