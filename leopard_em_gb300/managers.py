@@ -24,7 +24,6 @@ File I/O (MRC, CSV) and YAML schema handling are not part of this package.
 from __future__ import annotations
 
 import math
-import warnings
 from dataclasses import dataclass, field
 from typing import Optional
 
@@ -205,6 +204,35 @@ class MatchTemplateResult:
     total_projections: int = 0
     total_orientations: int = 0
     total_defocus: int = 0
+    allow_file_overwrite: bool = False
+    mip_path: str = ""
+    scaled_mip_path: str = ""
+    correlation_average_path: str = ""
+    correlation_variance_path: str = ""
+    orientation_psi_path: str = ""
+    orientation_theta_path: str = ""
+    orientation_phi_path: str = ""
+    relative_defocus_path: str = ""
+
+    MAPS = ("mip", "scaled_mip", "correlation_average", "correlation_variance", "orientation_psi",
+            "orientation_theta", "orientation_phi", "relative_defocus")
+
+    def export_results(self) -> None:
+        """Write the eight maps to their MRC paths (match_template_result.py:308-340)."""
+        from .mrc import write_mrc
+
+        for name in self.MAPS:
+            path = getattr(self, f"{name}_path")
+            if not path:
+                raise ValueError(f"{name}_path is not set")
+            write_mrc(path, getattr(self, name), overwrite=self.allow_file_overwrite)
+
+    def load_tensors_from_paths(self) -> None:
+        """Read the eight maps back from their MRC paths (match_template_result.py:238-250)."""
+        from .mrc import read_mrc
+
+        for name in self.MAPS:
+            setattr(self, name, torch.from_numpy(read_mrc(getattr(self, f"{name}_path"))).to(torch.float32))
 
     def apply_valid_cropping(self, template_shape) -> None:
         """Crop every map to (H - h + 1, W - w + 1) (match_template_result.py:206-236)."""
@@ -309,8 +337,7 @@ class MatchTemplateManager:
             nx = self.template_volume.shape[-1]
             r.apply_valid_cropping((nx, nx))
         if do_result_export:
-            warnings.warn("result export (MRC files) is not part of leopard_em_gb300; results stay in memory",
-                          stacklevel=2)
+            r.export_results()
 
 
 @dataclass
