@@ -53,6 +53,22 @@ static int colpass_t(const void* A, const void* Ip, int h, int Wcp, int n_c, int
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
+template <int HN>
+static int colpass_tab_t(const void* A, const void* Ip, int h, int Wcp, int n_c, int cpi, int y_rows, int waves,
+                         void* Y, cudaStream_t s) {
+  using CT = ColTab<HN>;
+  if (cudaFuncSetAttribute(colpass_tab_kernel<HN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CT::SMEM) !=
+      cudaSuccess)
+    return LGB_ERR_CUDA;
+  int per = 1;
+  const int groups = Wcp / CT::G;
+  const int split = colpass_split(groups, n_c, waves, &per);
+  colpass_tab_kernel<HN><<<dim3(groups, split), CT::G * CT::NT, CT::SMEM, s>>>(
+      static_cast<const float2*>(A), static_cast<const float2*>(Ip), h, Wcp, n_c, per, cpi, y_rows,
+      static_cast<float2*>(Y));
+  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+}
+
 template <int R, int P>
 static int colpass_fused_t(const void* A, const void* Ip, int h, int Wcp, int n_c, int cpi, int y_rows, int waves,
                            void* Y, cudaStream_t s) {
@@ -88,7 +104,7 @@ int launch_colpass(int H, const void* A, const void* Ip, int h, int Wcp, int n_c
   switch (H) {
 #define X(n) \
   case n:    \
-    return colpass_t<n>(A, Ip, h, Wcp, n_c, cpi, y_rows, waves, Y, s);
+    return colpass_tab_t<n>(A, Ip, h, Wcp, n_c, cpi, y_rows, waves, Y, s);
     LGB_COL_SIZES(X)
 #undef X
     default:

@@ -365,6 +365,71 @@ __global__ void __launch_bounds__(ColFused<R, P>::THREADS, 1)
 }
 
 // ---------------------------------------------------------------------------
+// Column pass for the mixed-radix lengths (those without a uniform R^P plan):
+// the generic Stockham schedule of Plan<HN> with the twiddles of every pass
+// after the first read from one shared table (filled once per CTA) instead
+// of sincospif per butterfly.  The forward first pass is pruned to the h
+// non-zero inputs.  G columns per CTA (ColGroupOf).
+// ---------------------------------------------------------------------------
+template <int HN>
+struct ColTab {
+  using RL = typename Plan<HN>::type;
+  static constexpr int NT = FftThreads<HN>::value;
+  static constexpr int G = ColGroupOf<HN>::value;
+  static constexpr int STRIDE = IdxPad16::pad(HN) + 4;
+  static constexpr int TAB = TableSize<1, RL>::value;
+  static constexpr size_t SMEM = sizeof(float2) * ((size_t)G * STRIDE + TAB);
+};
+
+template <int HN>
+__global__ void __launch_bounds__(ColTab<HN>::G* ColTab<HN>::NT, 1)
+    colpass_tab_kernel(const float2* __restrict__ A, const float2* __restrict__ Ip, int h, int Wcp, int n_c,
+                       int c_per_block, int c_per_image, int y_rows, float2* __restrict__ Y) {
+  using CT = ColTab<HN>;
+  using RL = typename CT::RL;
+  constexpr int NT = CT::NT, G = CT::G, STRIDE = CT::STRIDE, NTH = G * NT;
+  constexpr int R1 = Head<RL>::value;
+  extern __shared__ float2 ctsm[];
+  float2* tab = ctsm + G * STRIDE;
+  FillTables<HN, 1, RL>::run(tab, threadIdx.x, NTH);
+  const int kx0 = blockIdx.x * G;
+  const int c_begin = blockIdx.y * c_per_block;
+  const int c_end = min(n_c, c_begin + c_per_block);
+  const int g = threadIdx.x / NT, t = threadIdx.x - (threadIdx.x / NT) * NT;
+  float2* x = ctsm + g * STRIDE;
+  __syncthreads();
+#pragma unroll 1
+  for (int c = c_begin; c < c_end; ++c) {
+    const float2* a = A + (size_t)c * h * Wcp + kx0;
+    for (int e = threadIdx.x; e < h * G; e += NTH) {
+      const int y = e / G, i = e % G;
+      ctsm[i * STRIDE + IdxPad16::f(y)] = a[(size_t)y * Wcp + i];
+    }
+    __syncthreads();
+    // forward: pruned first pass (no twiddles), then the table passes
+    stockham_pass<HN, R1, 1, NT, -1, IdxPad16, true>(x, t, h);
+    TablePasses<HN, NT, -1, IdxPad16, R1, typename Tail<RL>::type>::run(x, tab, t);
+    const float2* ipc = Ip + (size_t)(c / c_per_image) * HN * Wcp;
+    for (int e = threadIdx.x; e < HN * G; e += NTH) {
+      const int y = e / G, i = e % G;
+      const float2 I = __ldg(ipc + (size_t)y * Wcp + kx0 + i);
+      const int si = i * STRIDE + IdxPad16::f(y);
+      float2 X = cmulc(I, ctsm[si]);
+      if (y == 0 && kx0 + i == 0) X = make_float2(0.f, 0.f);
+      ctsm[si] = X;
+    }
+    __syncthreads();
+    TablePasses<HN, NT, +1, IdxPad16, 1, RL>::run(x, tab, t);
+    float2* yo = Y + (size_t)c * y_rows * Wcp + kx0;
+    for (int e = threadIdx.x; e < y_rows * G; e += NTH) {
+      const int y = e / G, i = e % G;
+      yo[(size_t)y * Wcp + i] = ctsm[i * STRIDE + IdxPad16::f(y)];
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Fused row pass (c2r of length 2*WH + statistics).
 // ---------------------------------------------------------------------------
 template <int WH, int NT, class RL>
