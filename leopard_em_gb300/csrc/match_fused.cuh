@@ -27,51 +27,6 @@
 
 namespace lgb {
 
-// ---- radix-list helpers ----------------------------------------------------
-template <class RL>
-struct Head;
-template <int R, int... Rs>
-struct Head<Radices<R, Rs...>> {
-  static constexpr int value = R;
-};
-template <class RL>
-struct Last;
-template <int R>
-struct Last<Radices<R>> {
-  static constexpr int value = R;
-};
-template <int R, int R2, int... Rs>
-struct Last<Radices<R, R2, Rs...>> {
-  static constexpr int value = Last<Radices<R2, Rs...>>::value;
-};
-template <int R, class RL>
-struct Prepend;
-template <int R, int... Rs>
-struct Prepend<R, Radices<Rs...>> {
-  using type = Radices<R, Rs...>;
-};
-template <class RL>
-struct DropLast;
-template <int R>
-struct DropLast<Radices<R>> {
-  using type = Radices<>;
-};
-template <int R, int R2, int... Rs>
-struct DropLast<Radices<R, R2, Rs...>> {
-  using type = typename Prepend<R, typename DropLast<Radices<R2, Rs...>>::type>::type;
-};
-template <class RL>
-struct Tail;
-template <int R, int... Rs>
-struct Tail<Radices<R, Rs...>> {
-  using type = Radices<Rs...>;
-};
-// middle passes: drop first and last
-template <class RL>
-struct Middle {
-  using type = typename DropLast<typename Tail<RL>::type>::type;
-};
-
 // ---- async copy helpers (16-byte cp.async, completion via wait_group) -------
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -107,24 +62,6 @@ static __constant__ float2 kRootsFwd16[16] = {
     {0.92387953251128674f, 0.38268343236508977f},
 };
 
-// Padded shared-memory access at base + q*STEP.  With IdxPad16 and STEP a
-// multiple of 16, f(base + q*STEP) = f(base) + q*(STEP + STEP/16): one index
-// computation and compile-time offsets for the whole butterfly.
-template <class IDX, int STEP>
-__device__ __forceinline__ int padded_at(int fbase, int base, int q) {
-  if constexpr (std::is_same<IDX, IdxPad16>::value && STEP % 16 == 0) {
-    return fbase + q * (STEP + STEP / 16);
-  } else {
-    return IDX::f(base + q * STEP);
-  }
-}
-// f(R*j + q) for q < R <= 16 and R | 16: R*j + (R*j >> 4) + q.
-template <int R>
-__device__ __forceinline__ int padded_first(int j) {
-  static_assert(16 % R == 0, "radix must divide 16");
-  return R * j + ((R * j) >> 4);
-}
-
 // Value of v that the compiler cannot treat as loop invariant: keeps per-row
 // address arithmetic inside the loop instead of holding 16 hoisted addresses.
 __device__ __forceinline__ int opaque(int v) {
@@ -132,106 +69,6 @@ __device__ __forceinline__ int opaque(int v) {
   asm volatile("mov.b32 %0, %1;" : "=r"(r) : "r"(v));
   return r;
 }
-
-// ---- twiddles from a shared table ------------------------------------------
-// table row for k: w^t = exp(-2 pi i k t / L), t = 1..R-1 (forward sign);
-// the inverse uses the conjugates.
-// Table of one Stockham pass (stride NS, radix R): entry (t, k) =
-// exp(-2 pi i k t / (NS R)) at tab[(t-1)*NS + k], t = 1..R-1, k < NS.  Lanes
-// reading consecutive k hit consecutive addresses (no bank conflicts); lanes
-// sharing k broadcast.  The inverse uses the conjugates.
-template <int R, int DIR, int NS>
-__device__ __forceinline__ void twiddle_from_table(float2* v, const float2* tab, int k) {
-#pragma unroll
-  for (int t = 1; t < R; ++t) {
-    const float2 w = tab[(t - 1) * NS + k];
-    v[t] = DIR < 0 ? cmul(v[t], w) : cmulc(v[t], w);
-  }
-}
-
-template <int NS, int R>
-__device__ __forceinline__ void fill_twiddles(float2* tab, int tid, int nthreads) {
-  constexpr int L = NS * R;
-  for (int e = tid; e < NS * (R - 1); e += nthreads) {
-    const int t = e / NS + 1, k = e % NS;
-    float s, c;
-    sincospif(2.0f * (float)((k * t) % L) / (float)L, &s, &c);
-    tab[e] = make_float2(c, -s);
-  }
-}
-
-// Shared-memory Stockham pass with table twiddles (in place, two barriers).
-template <int N, int R, int NS, int NT, int DIR, class IDX>
-__device__ __forceinline__ void table_pass(float2* __restrict__ x, const float2* __restrict__ tab, int t) {
-  constexpr int NB = N / R;
-  constexpr int PER = (NB + NT - 1) / NT;
-  float2 v[PER][R];
-#pragma unroll
-  for (int p = 0; p < PER; ++p) {
-    const int j = t + p * NT;
-    if ((NB % NT == 0) || j < NB) {
-      const int fj = IDX::f(j);
-#pragma unroll
-      for (int q = 0; q < R; ++q) v[p][q] = x[padded_at<IDX, NB>(fj, j, q)];
-      if (NS > 1) twiddle_from_table<R, DIR, NS>(v[p], tab, j % NS);
-      Dft<R, DIR>::run(v[p]);
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int p = 0; p < PER; ++p) {
-    const int j = t + p * NT;
-    if ((NB % NT == 0) || j < NB) {
-      const int base = (j / NS) * NS * R + (j % NS);
-      const int fb = IDX::f(base);
-#pragma unroll
-      for (int q = 0; q < R; ++q) x[padded_at<IDX, NS>(fb, base, q)] = v[p][q];
-    }
-  }
-  __syncthreads();
-}
-
-// Table offsets: pass with stride NS starts at sum over earlier passes of NS'*(R'-1).
-template <int NS, class RL>
-struct TableSize;
-template <int NS>
-struct TableSize<NS, Radices<>> {
-  static constexpr int value = 0;
-};
-template <int NS, int R, int... Rs>
-struct TableSize<NS, Radices<R, Rs...>> {
-  static constexpr int value = (NS > 1 ? NS * (R - 1) : 0) + TableSize<NS * R, Radices<Rs...>>::value;
-};
-
-template <int N, int NS, class RL>
-struct FillTables;
-template <int N, int NS>
-struct FillTables<N, NS, Radices<>> {
-  static __device__ __forceinline__ void run(float2*, int, int) {}
-};
-template <int N, int NS, int R, int... Rs>
-struct FillTables<N, NS, Radices<R, Rs...>> {
-  static __device__ __forceinline__ void run(float2* tab, int tid, int nt) {
-    if (NS > 1) fill_twiddles<NS, R>(tab, tid, nt);
-    FillTables<N, NS * R, Radices<Rs...>>::run(tab + (NS > 1 ? NS * (R - 1) : 0), tid, nt);
-  }
-};
-
-// Run a list of middle passes (shared memory in place), starting at stride NS,
-// with twiddles from `tab` (laid out by TableSize/FillTables from stride NS0).
-template <int N, int NT, int DIR, class IDX, int NS, class RL>
-struct TablePasses;
-template <int N, int NT, int DIR, class IDX, int NS>
-struct TablePasses<N, NT, DIR, IDX, NS, Radices<>> {
-  static __device__ __forceinline__ void run(float2*, const float2*, int) {}
-};
-template <int N, int NT, int DIR, class IDX, int NS, int R, int... Rs>
-struct TablePasses<N, NT, DIR, IDX, NS, Radices<R, Rs...>> {
-  static __device__ __forceinline__ void run(float2* x, const float2* tab, int t) {
-    table_pass<N, R, NS, NT, DIR, IDX>(x, tab, t);
-    TablePasses<N, NT, DIR, IDX, NS * R, Radices<Rs...>>::run(x, tab + (NS > 1 ? NS * (R - 1) : 0), t);
-  }
-};
 
 // ---------------------------------------------------------------------------
 // Fused column pass for H = R^P.

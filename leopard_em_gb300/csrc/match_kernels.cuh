@@ -305,6 +305,12 @@ __global__ void __launch_bounds__(ColGroupOf<HN>::value* FftThreads<HN>::value, 
 // ---------------------------------------------------------------------------
 constexpr int kRowThreads = 256;
 
+template <int WH>
+struct RowGeneric {
+  static constexpr size_t SMEM = sizeof(float2) * ((size_t)WH + 4 + IdxPad16::pad(WH) + 2 + WH +
+                                                   FftTable<WH>::SIZE + 1);
+};
+
 // Largest divisor of WH that is <= kRowThreads (threads of one rowpass CTA).
 constexpr int row_threads(int wh, int cand = kRowThreads) {
   return cand <= 1 ? 1 : (wh % cand == 0 ? cand : row_threads(wh, cand - 1));
@@ -319,10 +325,21 @@ __global__ void __launch_bounds__(NT, 2)
   static_assert(WH % NT == 0, "row length must be a multiple of the CTA size");
   constexpr int PIX = WH / NT;
   constexpr int ZS = IdxPad16::pad(WH) + 2;
-  __shared__ float2 xr[WH + 4];
-  __shared__ float2 z[ZS];
+  // dynamic shared memory (RowGeneric<WH>::SMEM): row, transform, c2r
+  // pre-twiddles and FFT twiddle table (filled once, reused by every correlogram)
+  extern __shared__ float2 rgsm[];
+  float2* xr = rgsm;
+  float2* z = xr + WH + 4;
+  float2* pre = z + ZS;
+  float2* tab = pre + WH;
   const int y = blockIdx.x;
   const int t = threadIdx.x;
+  fill_fft_table<WH>(tab, t, NT);
+  for (int k = t; k < WH; k += NT) {
+    float sn, cs;
+    sincospif((float)k / (float)WH, &sn, &cs);
+    pre[k] = make_float2(cs, sn);
+  }
   float bmax[2 * PIX], bs[2 * PIX], bss[2 * PIX];
   int barg[2 * PIX];
 #pragma unroll
@@ -342,13 +359,11 @@ __global__ void __launch_bounds__(NT, 2)
       if (k == 0) { A.y = 0.f; B.y = 0.f; }
       B.y = -B.y;
       const float2 xe = cadd(A, B);
-      float sn, cs;
-      sincospif((float)k / (float)WH, &sn, &cs);
-      const float2 xo = cmul(csub(A, B), make_float2(cs, sn));
+      const float2 xo = cmul(csub(A, B), pre[k]);
       z[IdxPad16::f(k)] = cadd(xe, mul_i<1>(xo));
     }
     __syncthreads();
-    block_fft_outline<WH, NT, +1, IdxPad16>(z, t);
+    block_fft_tab<WH, NT, +1, IdxPad16>(z, tab, t);
 #pragma unroll
     for (int r = 0; r < PIX; ++r) {
       const float2 v = z[IdxPad16::f(t + r * NT)];

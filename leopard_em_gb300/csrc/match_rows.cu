@@ -42,9 +42,13 @@ template <int WH>
 static int rowpass_t(const void* Y, int H, int y_rows, int Wcp, int n_c, int nb, int n_orient, int o0,
                      const int* o0_dev, float* mip, int* best, double* s1, double* s2, cudaStream_t s) {
   constexpr int NT = row_threads(WH);
+  constexpr size_t SMEM = RowGeneric<WH>::SMEM;
+  if (cudaFuncSetAttribute(rowpass_kernel<WH, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM) !=
+      cudaSuccess)
+    return LGB_ERR_CUDA;
   const float scale = 1.0f / ((float)H * (float)(2 * WH));
-  rowpass_kernel<WH, NT><<<y_rows, NT, 0, s>>>(static_cast<const float2*>(Y), y_rows, Wcp, n_c, nb, n_orient, o0,
-                                               o0_dev, scale, mip, best, s1, s2);
+  rowpass_kernel<WH, NT><<<y_rows, NT, SMEM, s>>>(static_cast<const float2*>(Y), y_rows, Wcp, n_c, nb, n_orient,
+                                                  o0, o0_dev, scale, mip, best, s1, s2);
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 

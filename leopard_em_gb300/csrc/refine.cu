@@ -108,9 +108,18 @@ __global__ void __launch_bounds__(NT)
   constexpr int ZS = IdxPad16::pad(WH) + 2;
   __shared__ float2 xr[WH + 4];
   __shared__ float2 z[ZS];
+  // c2r pre-twiddles and FFT twiddles, filled once and reused by every correlogram
+  __shared__ float2 pre[WH];
+  __shared__ float2 tab[FftTable<WH>::SIZE + 1];
   __shared__ unsigned long long red_key[1];
   __shared__ unsigned red_cc[1];
   const int y = blockIdx.x, p = blockIdx.y, t = threadIdx.x;
+  fill_fft_table<WH>(tab, t, NT);
+  for (int k = t; k < WH; k += NT) {
+    float sn, cs;
+    sincospif((float)k / (float)WH, &sn, &cs);
+    pre[k] = make_float2(cs, sn);
+  }
   unsigned long long best_key = 0ull;
   unsigned best_cc = 0u;
   const float* mrow = corr_mean + ((size_t)p * crop_h + y) * crop_w;
@@ -124,13 +133,11 @@ __global__ void __launch_bounds__(NT)
       float2 B = xr[WH - k];
       if (k == 0) { A.y = 0.f; B.y = 0.f; }
       B.y = -B.y;
-      float sn, cs;
-      sincospif((float)k / (float)WH, &sn, &cs);
-      const float2 xo = cmul(csub(A, B), make_float2(cs, sn));
+      const float2 xo = cmul(csub(A, B), pre[k]);
       z[IdxPad16::f(k)] = cadd(cadd(A, B), mul_i<1>(xo));
     }
     __syncthreads();
-    block_fft<WH, NT, +1, IdxPad16>(z, t);
+    block_fft_tab<WH, NT, +1, IdxPad16>(z, tab, t);
     for (int m = t; 2 * m < crop_w; m += NT) {
       const float2 v = z[IdxPad16::f(m)];
 #pragma unroll
