@@ -123,7 +123,10 @@ __global__ void __launch_bounds__(ROWS* FftThreads<HT / 2>::value)
   const int py = (y + HT - HT / 2) % HT;
   const float scale = 1.0f / ((float)HT * (float)HT);
   const bool edge_row = (py == 0) || (py == HT - 1);
-  double s1 = 0.0, s2 = 0.0, se = 0.0;
+  // per-thread partial moments of <= M/NT pixel pairs in FP32 (FP64 arithmetic
+  // is a small fraction of the FP32 rate on this GPU); the cross-thread and
+  // cross-row reductions are FP64
+  float s1 = 0.f, s2 = 0.f, se = 0.f;
   float* prow = proj + ((size_t)c * HT + py) * HT;
   for (int m = t; m < M; m += NT) {
     const float2 v = z[g][IdxPad16::f(m)];
@@ -131,18 +134,18 @@ __global__ void __launch_bounds__(ROWS* FftThreads<HT / 2>::value)
     const int px0 = (2 * m + HT - HT / 2) % HT, px1 = (2 * m + 1 + HT - HT / 2) % HT;
     prow[px0] = a;
     prow[px1] = b;
-    s1 += (double)a + (double)b;
-    s2 += (double)a * a + (double)b * b;
+    s1 += a + b;
+    s2 = fmaf(a, a, fmaf(b, b, s2));
     if (edge_row) {
-      se += (double)a + (double)b;
+      se += a + b;
     } else {
       if (px0 == 0 || px0 == HT - 1) se += a;
       if (px1 == 0 || px1 == HT - 1) se += b;
     }
   }
-  part[threadIdx.x][0] = s1;
-  part[threadIdx.x][1] = s2;
-  part[threadIdx.x][2] = se;
+  part[threadIdx.x][0] = (double)s1;
+  part[threadIdx.x][1] = (double)s2;
+  part[threadIdx.x][2] = (double)se;
   __syncthreads();
   if (t == 0) {
     double a = 0, b = 0, e = 0;
