@@ -209,12 +209,11 @@ __global__ void __launch_bounds__(ROWS* FftThreads<WH>::value)
   constexpr int NT = FftThreads<WH>::value;
   constexpr int ZS = IdxPad16::pad(WH) + 2;
   __shared__ float2 z[ROWS][ZS];
-  __shared__ float norm[2];
   const int c = blockIdx.y;
-  if (threadIdx.x < 32)
-    projection_norm_constants(rowstats + (size_t)c * h * 3, h, norm_h, norm_w, &norm[0], &norm[1]);
-  __syncthreads();
-  const float e = norm[0], s = norm[1];
+  // constants from norm_constants_kernel (rowstats[c][0][0..1])
+  const float e = (float)rowstats[(size_t)c * h * 3], s = (float)rowstats[(size_t)c * h * 3 + 1];
+  (void)norm_h;
+  (void)norm_w;
   const int g = threadIdx.x / NT, t = threadIdx.x - (threadIdx.x / NT) * NT;
   const int y = blockIdx.x * ROWS + g;
   const bool active = y < h;

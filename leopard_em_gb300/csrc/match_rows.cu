@@ -6,6 +6,24 @@
 
 namespace lgb {
 
+// One warp per correlogram: the normalisation constants (edge mean, scale)
+// from the h row moments, stored as two doubles over rowstats[c][0][0..1]
+// (row 0's moments are not needed afterwards), so that every pad_rfft CTA
+// reads them instead of reducing all rows again.
+__global__ void norm_constants_kernel(double* __restrict__ rowstats, int n_c, int h, int norm_h, int norm_w) {
+  const int c = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  if (c >= n_c) return;
+  double* rs = rowstats + (size_t)c * h * 3;
+  float e = 0.f, s = 0.f;
+  projection_norm_constants(rs, h, norm_h, norm_w, &e, &s);
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) {
+    rs[0] = (double)e;
+    rs[1] = (double)s;
+  }
+}
+
+
 // W/2 values
 #define LGB_ROW_SIZES(X) \
   X(24) X(32) X(40) X(64) X(128) X(144) X(256) X(288) X(512) X(1024) X(1440) X(1536) X(1920) X(2048) X(2880)
@@ -55,6 +73,10 @@ static int rowpass_t(const void* Y, int H, int y_rows, int Wcp, int n_c, int nb,
 int launch_pad_rfft(int W, const float* proj, const double* rowstats, int h, int norm_h, int norm_w, int Wcp,
                     int n_c, void* A, cudaStream_t s) {
   if (W % 2 || norm_w > W || norm_w < h || norm_h < h) return LGB_ERR_UNSUPPORTED_SIZE;
+  if (!supported_row(W)) return LGB_ERR_UNSUPPORTED_SIZE;
+  // normalisation constants once per correlogram (8 warps per CTA)
+  norm_constants_kernel<<<(n_c + 7) / 8, 256, 0, s>>>(const_cast<double*>(rowstats), n_c, h, norm_h, norm_w);
+  if (cudaGetLastError() != cudaSuccess) return LGB_ERR_CUDA;
   switch (W / 2) {
 #define X(n) \
   case n:    \
