@@ -102,9 +102,10 @@ __device__ __forceinline__ float unord_f(unsigned u) {
 // reference's torch.max over correlograms and then over pixels resolves ties.
 template <int WH, int NT>
 __global__ void __launch_bounds__(NT)
-    refine_rowpass_kernel(const float2* __restrict__ Y, int y_rows, int Wcp, int n_cpp, int crop_w, float scale,
-                          const float* __restrict__ corr_mean, const float* __restrict__ corr_std, int crop_h,
-                          unsigned long long* __restrict__ slot_key, unsigned* __restrict__ slot_cc) {
+    refine_rowpass_kernel(const float2* __restrict__ Y, int y_rows, int Wcp, int n_cpp, int c_per_block,
+                          int crop_w, float scale, const float* __restrict__ corr_mean,
+                          const float* __restrict__ corr_std, int crop_h, unsigned long long* __restrict__ slot_key,
+                          unsigned* __restrict__ slot_cc) {
   constexpr int ZS = IdxPad16::pad(WH) + 2;
   __shared__ float2 xr[WH + 4];
   __shared__ float2 z[ZS];
@@ -124,7 +125,11 @@ __global__ void __launch_bounds__(NT)
   unsigned best_cc = 0u;
   const float* mrow = corr_mean + ((size_t)p * crop_h + y) * crop_w;
   const float* srow = corr_std + ((size_t)p * crop_h + y) * crop_w;
-  for (int c = 0; c < n_cpp; ++c) {
+  // this CTA's share of the particle's correlograms (blockIdx.z); the slots
+  // combine the shares with atomicMax
+  const int c_begin = blockIdx.z * c_per_block;
+  const int c_end = min(n_cpp, c_begin + c_per_block);
+  for (int c = c_begin; c < c_end; ++c) {
     const float2* row = Y + (((size_t)p * n_cpp + c) * y_rows + y) * Wcp;
     for (int k = t; k <= WH; k += NT) xr[k] = row[k];
     __syncthreads();
@@ -223,9 +228,18 @@ static int refine_rowpass_t(const void* Y, int y_rows, int Wcp, int n_cpp, int P
                             float scale, const float* mean, const float* std_, unsigned long long* key, unsigned* cc,
                             cudaStream_t s) {
   constexpr int NT = row_threads(WH);
-  dim3 grid(crop_h, P);
-  refine_rowpass_kernel<WH, NT><<<grid, NT, 0, s>>>(static_cast<const float2*>(Y), y_rows, Wcp, n_cpp, crop_w, scale,
-                                                    mean, std_, crop_h, key, cc);
+  // split each particle's correlograms until the grid covers ~4 waves of the SMs
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int split = 1;
+  while (split < n_cpp && crop_h * P * split < 4 * sms) split *= 2;
+  if (split > n_cpp) split = n_cpp;
+  const int per = (n_cpp + split - 1) / split;
+  split = (n_cpp + per - 1) / per;
+  dim3 grid(crop_h, P, split);
+  refine_rowpass_kernel<WH, NT><<<grid, NT, 0, s>>>(static_cast<const float2*>(Y), y_rows, Wcp, n_cpp, per, crop_w,
+                                                    scale, mean, std_, crop_h, key, cc);
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
