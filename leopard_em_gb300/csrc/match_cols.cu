@@ -61,7 +61,7 @@ static int colpass_tab_t(const void* A, const void* Ip, int h, int Wcp, int n_c,
       cudaSuccess)
     return LGB_ERR_CUDA;
   int per = 1;
-  const int groups = Wcp / CT::G;
+  const int groups = (Wcp + CT::G - 1) / CT::G;
   const int split = colpass_split(groups, n_c, waves, &per);
   colpass_tab_kernel<HN><<<dim3(groups, split), CT::G * CT::NT, CT::SMEM, s>>>(
       static_cast<const float2*>(A), static_cast<const float2*>(Ip), h, Wcp, n_c, per, cpi, y_rows,

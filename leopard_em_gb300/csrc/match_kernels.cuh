@@ -205,15 +205,24 @@ __device__ inline void projection_norm_constants(const double* rs, int h, int H,
 template <int WH, int ROWS>
 __global__ void __launch_bounds__(ROWS* FftThreads<WH>::value)
     pad_rfft_kernel(const float* __restrict__ proj, const double* __restrict__ rowstats, int h, int norm_h,
-                    int norm_w, int Wcp, float2* __restrict__ A) {
+                    int norm_w, int Wcp, int norm_ready, float2* __restrict__ A) {
   constexpr int NT = FftThreads<WH>::value;
   constexpr int ZS = IdxPad16::pad(WH) + 2;
   __shared__ float2 z[ROWS][ZS];
   const int c = blockIdx.y;
-  // constants from norm_constants_kernel (rowstats[c][0][0..1])
-  const float e = (float)rowstats[(size_t)c * h * 3], s = (float)rowstats[(size_t)c * h * 3 + 1];
-  (void)norm_h;
-  (void)norm_w;
+  // norm_ready: constants precomputed by norm_constants_kernel in
+  // rowstats[c][0][0..1]; otherwise warp 0 reduces the row moments here
+  __shared__ float norm[2];
+  if (norm_ready) {
+    if (threadIdx.x == 0) {
+      norm[0] = (float)rowstats[(size_t)c * h * 3];
+      norm[1] = (float)rowstats[(size_t)c * h * 3 + 1];
+    }
+  } else if (threadIdx.x < 32) {
+    projection_norm_constants(rowstats + (size_t)c * h * 3, h, norm_h, norm_w, &norm[0], &norm[1]);
+  }
+  __syncthreads();
+  const float e = norm[0], s = norm[1];
   const int g = threadIdx.x / NT, t = threadIdx.x - (threadIdx.x / NT) * NT;
   const int y = blockIdx.x * ROWS + g;
   const bool active = y < h;

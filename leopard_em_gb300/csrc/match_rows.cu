@@ -50,8 +50,16 @@ static int pad_rfft_t(const float* proj, const double* rowstats, int h, int norm
   // static shared memory (ROWS rows of the padded transform) stays under 40 KB
   constexpr int ROWS = ROWS1 * (IdxPad16::pad(WH) + 2) * 8 <= 40960 ? ROWS1 : 1;
   static_assert(ROWS * NT >= 32, "pad_rfft CTA must hold a full warp");
-  dim3 grid((h + ROWS - 1) / ROWS, n_c);
-  pad_rfft_kernel<WH, ROWS><<<grid, ROWS * NT, 0, s>>>(proj, rowstats, h, norm_h, norm_w, Wcp,
+  const int ctas = (h + ROWS - 1) / ROWS;
+  // precompute the constants when many CTAs share a correlogram (each would
+  // otherwise reduce all h rows in FP64); a few CTAs do it themselves
+  const int ready = ctas >= 16;
+  if (ready) {
+    norm_constants_kernel<<<(n_c + 7) / 8, 256, 0, s>>>(const_cast<double*>(rowstats), n_c, h, norm_h, norm_w);
+    if (cudaGetLastError() != cudaSuccess) return LGB_ERR_CUDA;
+  }
+  dim3 grid(ctas, n_c);
+  pad_rfft_kernel<WH, ROWS><<<grid, ROWS * NT, 0, s>>>(proj, rowstats, h, norm_h, norm_w, Wcp, ready,
                                                        static_cast<float2*>(A));
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
@@ -74,9 +82,6 @@ int launch_pad_rfft(int W, const float* proj, const double* rowstats, int h, int
                     int n_c, void* A, cudaStream_t s) {
   if (W % 2 || norm_w > W || norm_w < h || norm_h < h) return LGB_ERR_UNSUPPORTED_SIZE;
   if (!supported_row(W)) return LGB_ERR_UNSUPPORTED_SIZE;
-  // normalisation constants once per correlogram (8 warps per CTA)
-  norm_constants_kernel<<<(n_c + 7) / 8, 256, 0, s>>>(const_cast<double*>(rowstats), n_c, h, norm_h, norm_w);
-  if (cudaGetLastError() != cudaSuccess) return LGB_ERR_CUDA;
   switch (W / 2) {
 #define X(n) \
   case n:    \
