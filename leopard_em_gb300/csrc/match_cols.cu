@@ -36,24 +36,6 @@ static int colpass_split(int groups, int n_c, int waves, int* per) {
 }
 
 template <int HN>
-static int colpass_t(const void* A, const void* Ip, int h, int Wcp, int n_c, int cpi, int y_rows, int waves, void* Y,
-                     cudaStream_t s) {
-  constexpr int NT = FftThreads<HN>::value;
-  constexpr int G = ColGroupOf<HN>::value;
-  const size_t smem = sizeof(float2) * G * (IdxPad16::pad(HN) + 4);
-  if (cudaFuncSetAttribute(colpass_kernel<HN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-      cudaSuccess)
-    return LGB_ERR_CUDA;
-  int per = 1;
-  const int groups = Wcp / G;
-  const int split = colpass_split(groups, n_c, waves, &per);
-  dim3 grid(groups, split);
-  colpass_kernel<HN><<<grid, G * NT, smem, s>>>(static_cast<const float2*>(A), static_cast<const float2*>(Ip), h, Wcp,
-                                                n_c, per, cpi, y_rows, static_cast<float2*>(Y));
-  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
-}
-
-template <int HN>
 static int colpass_tab_t(const void* A, const void* Ip, int h, int Wcp, int n_c, int cpi, int y_rows, int waves,
                          void* Y, cudaStream_t s) {
   using CT = ColTab<HN>;

@@ -9,9 +9,9 @@
 //   proj_row_kernel   c2r along x, 1/d^2, ifftshift, per-row moments    [n_c, d, d]
 //   pad_rfft_kernel   edge-mean/variance normalisation (utils.py:106-188)
 //                     and the zero-padded row rfft of length W          [n_c, d, Wcp]
-//   colpass_kernel    per column: pruned FFT along y (length H), cross power
+//   column pass       per column: pruned FFT along y (length H), cross power
 //                     image * conj(P) with P[0,0]=0, inverse FFT along y
-//                                                                      [n_c, H, Wcp]
+//                     (colpass_fused_kernel / colpass_tab_kernel)      [n_c, H, Wcp]
 //   rowpass_kernel    per row: c2r of length W (1/(H W)) and the fused
 //                     statistics update (utils.py:191-255): max over the
 //                     batch, strict '>' MIP update, global index, FP64 sums
@@ -251,62 +251,12 @@ __global__ void __launch_bounds__(ROWS* FftThreads<WH>::value)
   for (int k = WH + 1 + t; k < Wcp; k += NT) out[k] = make_float2(0.f, 0.f);
 }
 
-// ---------------------------------------------------------------------------
-// colpass: per group of 4 columns, for each correlogram c in this CTA's range:
-//   P = FFT_y(A_c[0..h), zero padded to HN);  X = I * conj(P), X[0,0] = 0;
-//   Y_c = IFFT_y(X)   (unscaled)
-// ---------------------------------------------------------------------------
 // Columns per colpass CTA: kColGroup, or 2 where four transforms of length HN
 // would need more than 1024 threads (HN = 5760).
 template <int HN>
 struct ColGroupOf {
   static constexpr int value = kColGroup * FftThreads<HN>::value <= 1024 ? kColGroup : 2;
 };
-
-template <int HN>
-__global__ void __launch_bounds__(ColGroupOf<HN>::value* FftThreads<HN>::value, 1)
-    colpass_kernel(const float2* __restrict__ A, const float2* __restrict__ Ip, int h, int Wcp, int n_c,
-                   int c_per_block, int c_per_image, int y_rows, float2* __restrict__ Y) {
-  constexpr int NT = FftThreads<HN>::value;
-  constexpr int G = ColGroupOf<HN>::value;
-  constexpr int STRIDE = IdxPad16::pad(HN) + 4;
-  extern __shared__ float2 cbuf[];
-  const int kx0 = blockIdx.x * G;
-  const int c_begin = blockIdx.y * c_per_block;
-  const int c_end = min(n_c, c_begin + c_per_block);
-  const int g = threadIdx.x / NT, t = threadIdx.x - (threadIdx.x / NT) * NT;
-  constexpr int NTH = G * NT;
-#pragma unroll 1
-  for (int c = c_begin; c < c_end; ++c) {
-    const float2* a = A + (size_t)c * h * Wcp + kx0;
-#pragma unroll 1
-    for (int e = threadIdx.x; e < h * G; e += NTH) {
-      const int y = e / G, i = e % G;
-      cbuf[i * STRIDE + IdxPad16::f(y)] = a[(size_t)y * Wcp + i];
-    }
-    __syncthreads();
-    block_fft_pruned_outline<HN, NT, -1, IdxPad16>(cbuf + g * STRIDE, t, h);
-    const float2* ipc = Ip + (size_t)(c / c_per_image) * HN * Wcp;
-#pragma unroll 2
-    for (int e = threadIdx.x; e < HN * G; e += NTH) {
-      const int y = e / G, i = e % G;
-      const float2 I = __ldg(ipc + (size_t)y * Wcp + kx0 + i);
-      const int si = i * STRIDE + IdxPad16::f(y);
-      float2 X = cmulc(I, cbuf[si]);
-      if (y == 0 && kx0 + i == 0) X = make_float2(0.f, 0.f);
-      cbuf[si] = X;
-    }
-    __syncthreads();
-    block_fft_outline<HN, NT, +1, IdxPad16>(cbuf + g * STRIDE, t);
-    float2* yo = Y + (size_t)c * y_rows * Wcp + kx0;
-#pragma unroll 2
-    for (int e = threadIdx.x; e < y_rows * G; e += NTH) {
-      const int y = e / G, i = e % G;
-      yo[(size_t)y * Wcp + i] = cbuf[i * STRIDE + IdxPad16::f(y)];
-    }
-    __syncthreads();
-  }
-}
 
 // ---------------------------------------------------------------------------
 // rowpass: row y of every correlogram in the batch: c2r of length W = 2*WH
