@@ -150,3 +150,34 @@ def test_gloo_two_ranks_gather_reduce(case, batch):
     torch.testing.assert_close(red["correlation_sum"], full["correlation_sum"], rtol=1e-12, atol=1e-12)
     torch.testing.assert_close(red["correlation_squared_sum"], full["correlation_squared_sum"], rtol=1e-12,
                                atol=1e-12)
+
+
+@pytest.mark.gpu
+def test_device_shards_reduce_to_the_full_search():
+    """Two orientation shards searched on the device, reduced in rank order and
+    finalised, equal one search over all orientations."""
+    from leopard_em_gb300 import synthetic as sy
+    from leopard_em_gb300.backend import MatchTemplateSearch
+
+    cfg = sy.MatchConfig(image_shape=(256, 256), template_size=32, n_blobs=60, blob_radius=11.0, n_particles=2,
+                         snr=0.5, seed=8, defocus_offsets=(-200.0, 0.0, 200.0))
+    eul = sy.uniform_euler_grid(30.0, 30.0)[:23]
+    kw = sy.make_match_workload(cfg, euler_angles=eul).kwargs
+    dev = torch.device("cuda:0")
+    full = MatchTemplateSearch(**kw, device=dev, orientation_batch_size=4)
+    full.run()
+    ref = full.result(to_cpu=True)
+    shards = []
+    for a, b in sharding.orientation_shards(23, 2, 4):
+        s = MatchTemplateSearch(**kw, device=dev, orientation_batch_size=4)
+        s.run(a, b)
+        shards.append({k: v.clone() for k, v in s.maps().items()})
+    red = sharding.reduce_search_maps(shards)
+    host = MatchTemplateSearch(**kw, device=dev, orientation_batch_size=4)
+    host.load_maps(red)
+    host.orientations_done = 23
+    got = host.result(to_cpu=True)
+    assert torch.equal(got["mip"], ref["mip"])
+    for k in ("best_phi", "best_theta", "best_psi", "best_defocus"):
+        assert torch.equal(got[k], ref[k]), k
+    torch.testing.assert_close(got["scaled_mip"], ref["scaled_mip"], rtol=1e-5, atol=1e-5)
