@@ -400,7 +400,9 @@ def learned_refine_bench(kw, dev, cfg, plain_res, n_plain):
         return {"learned": None}
     net = pr.ProposalNet(dev)
     pr.load_weights(net, path)
-    small = sy.local_euler_offsets(1.0, 0.25, 1.0, 0.25)
+    # +-0.5 deg at 0.125 deg: the same 576 offsets as +-1 deg at 0.25 deg, measured
+    # higher mean refined SNR than the plain grid (the proposals are within ~0.2 deg)
+    small = sy.local_euler_offsets(0.5, 0.125, 0.5, 0.125)
     small_df = torch.arange(-100.0, 100.0 + 1e-6, 50.0)
     res, info = pr.refine_with_proposals(net, kw, dev, small, small_df, batch_size=cfg.batch)
     out = {"learned_mean_refined_snr": float(res["refined_z_score"].mean()),
@@ -419,7 +421,7 @@ def learned_refine_bench(kw, dev, cfg, plain_res, n_plain):
                       "fallbacks": info_big["fallback"],
                       "correlations_per_particle": info_big["correlations_per_particle"],
                       "mean_refined_snr": float(res_big["refined_z_score"].mean()),
-                      "small_grid": "+-1 deg @ 0.25 x +-100 A @ 50",
+                      "small_grid": "+-0.5 deg @ 0.125 x +-100 A @ 50",
                       "timing": "wall clock, host tensors in and out (includes network inputs, inference, "
                                 "two refinement calls and any fallback)"}
     return out

@@ -126,7 +126,8 @@ def test_learned_proposals_match_plain_grid_snr_with_fewer_correlations():
     plain = core_refine_template(**kw, device=torch.device("cuda:0"), batch_size=cfg.batch)
     net = pr.ProposalNet(torch.device("cuda:0"))
     pr.load_weights(net, path)
-    res, info = pr.refine_with_proposals(net, kw, torch.device("cuda:0"), sy.local_euler_offsets(1.0, 0.25, 1.0, 0.25),
+    small = sy.local_euler_offsets(0.5, 0.125, 0.5, 0.125)
+    res, info = pr.refine_with_proposals(net, kw, torch.device("cuda:0"), small,
                                          torch.arange(-100.0, 100.0 + 1e-6, 50.0), batch_size=cfg.batch)
     zp, zl = plain["refined_z_score"].mean().item(), res["refined_z_score"].mean().item()
     print(f"mean refined SNR plain {zp:.3f} learned {zl:.3f}; correlograms/particle "
