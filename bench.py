@@ -65,6 +65,8 @@ def _args():
     ap.add_argument("--refine-particles", type=int, default=8)
     ap.add_argument("--no-refine", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--refine-plain-only", action="store_true",
+                    help="only time the plain refinement grid on --refine-particles particles (profiling)")
     ap.add_argument("--no-precision", action="store_true")
     ap.add_argument("--precision-error-orient", type=int, default=256,
                     help="orientations of the small configuration checked against the FP64 oracle")
@@ -338,6 +340,30 @@ def batched_bench(args, dev):
     }
 
 
+def refine_plain_only(args):
+    """Plain refinement grid alone (device-timed particles/s), for profiling."""
+    from leopard_em_gb300 import synthetic as sy
+    from leopard_em_gb300.backend.core_refine_template import refine_particles_device
+
+    dev = torch.device("cuda", 0)
+    cfg = sy.CONFIG_REFINE
+    n = args.refine_particles
+    kw, _ = sy.make_refine_workload(cfg, n, device=dev)
+    dkw = {k: (v.to(dev) if isinstance(v, torch.Tensor) else v) for k, v in kw.items()}
+    warm = dict(dkw)
+    warm["euler_angle_offsets"] = dkw["euler_angle_offsets"][: 2 * cfg.batch]
+    refine_particles_device(**warm, device=dev, batch_size=cfg.batch)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    refine_particles_device(**dkw, device=dev, batch_size=cfg.batch)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    return {"metric": "refined particles/s (plain local grid)", "value": n / (e0.elapsed_time(e1) / 1e3),
+            "unit": "particles/s", "particles": n, "workload": cfg.name}
+
+
 def refine_bench(args, dev, with_cpu):
     """Refined particles/s of the plain local grid (288^2 crops, 256^3 template,
     +-3 deg @ 0.25 deg x +-400 A @ 50 A)."""
@@ -463,6 +489,9 @@ def main():
     args = _args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.refine_plain_only:
+        print(json.dumps(refine_plain_only(args)), flush=True)
         return
     rank, world, local = _dist()
     if world > 1 and not torch.distributed.is_initialized():
