@@ -513,5 +513,12 @@ template <int N, int NT, int DIR, class IDX = IdxPlain>
 __device__ __forceinline__ void block_fft_tab(float2* x, const float2* tab, int t) {
   TablePasses<N, NT, DIR, IDX, 1, typename Plan<N>::type>::run(x, tab, t);
 }
+// Same, with inputs at index >= nz known to be zero (the first pass skips them).
+template <int N, int NT, int DIR, class IDX = IdxPlain>
+__device__ __forceinline__ void block_fft_pruned_tab(float2* x, const float2* tab, int t, int nz) {
+  using RL = typename Plan<N>::type;
+  stockham_pass<N, Head<RL>::value, 1, NT, DIR, IDX, true>(x, t, nz);
+  TablePasses<N, NT, DIR, IDX, Head<RL>::value, typename Tail<RL>::type>::run(x, tab, t);
+}
 
 }  // namespace lgb

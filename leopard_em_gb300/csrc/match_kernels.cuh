@@ -202,13 +202,25 @@ __device__ inline void projection_norm_constants(const double* rs, int h, int H,
 // zero padded to a supported FFT length).  Real FFT of length W = 2*WH through a
 // WH-point complex FFT (first pass pruned to the ceil(h/2) non-zero inputs).
 // ---------------------------------------------------------------------------
-template <int WH, int ROWS>
+// TAB: twiddles and post-twiddles from shared tables filled once per CTA (for
+// small transforms, where a CTA holds many rows to amortise the fill).
+template <int WH, int ROWS, bool TAB>
 __global__ void __launch_bounds__(ROWS* FftThreads<WH>::value)
     pad_rfft_kernel(const float* __restrict__ proj, const double* __restrict__ rowstats, int h, int norm_h,
                     int norm_w, int Wcp, int norm_ready, float2* __restrict__ A) {
   constexpr int NT = FftThreads<WH>::value;
   constexpr int ZS = IdxPad16::pad(WH) + 2;
   __shared__ float2 z[ROWS][ZS];
+  __shared__ float2 post[TAB ? WH + 1 : 1];  // exp(-i pi k / WH)
+  __shared__ float2 tab[TAB ? FftTable<WH>::SIZE + 1 : 1];
+  if (TAB) {
+    fill_fft_table<WH>(tab, threadIdx.x, blockDim.x);
+    for (int k = threadIdx.x; k <= WH; k += blockDim.x) {
+      float sn, cs;
+      sincospif((float)k / (float)WH, &sn, &cs);
+      post[k] = make_float2(cs, -sn);
+    }
+  }
   const int c = blockIdx.y;
   // norm_ready: constants precomputed by norm_constants_kernel in
   // rowstats[c][0][0..1]; otherwise warp 0 reduces the row moments here
@@ -236,7 +248,10 @@ __global__ void __launch_bounds__(ROWS* FftThreads<WH>::value)
     }
   }
   __syncthreads();
-  block_fft_pruned<WH, NT, -1, IdxPad16>(z[g], t, nz);
+  if (TAB)
+    block_fft_pruned_tab<WH, NT, -1, IdxPad16>(z[g], tab, t, nz);
+  else
+    block_fft_pruned<WH, NT, -1, IdxPad16>(z[g], t, nz);
   if (!active) return;
   float2* out = A + ((size_t)c * h + y) * Wcp;
   for (int k = t; k <= WH; k += NT) {
@@ -244,9 +259,15 @@ __global__ void __launch_bounds__(ROWS* FftThreads<WH>::value)
     const float2 Zm = cconj(z[g][IdxPad16::f(k == 0 ? 0 : WH - k)]);
     const float2 xe = cscale(cadd(Zk, Zm), 0.5f);
     const float2 xo = mul_i<-1>(cscale(csub(Zk, Zm), 0.5f));
-    float sn, cs;
-    sincospif((float)k / (float)WH, &sn, &cs);
-    out[k] = cadd(xe, cmul(make_float2(cs, -sn), xo));
+    float2 w;
+    if (TAB) {
+      w = post[k];
+    } else {
+      float sn, cs;
+      sincospif((float)k / (float)WH, &sn, &cs);
+      w = make_float2(cs, -sn);
+    }
+    out[k] = cadd(xe, cmul(w, xo));
   }
   for (int k = WH + 1 + t; k < Wcp; k += NT) out[k] = make_float2(0.f, 0.f);
 }

@@ -45,7 +45,7 @@ static int pad_rfft_t(const float* proj, const double* rowstats, int h, int norm
                       void* A, cudaStream_t s) {
   constexpr int NT = FftThreads<WH>::value;
   // at least one full warp: the normalisation reduction shuffles across warp 0
-  constexpr int ROWS0 = NT >= 128 ? 2 : (NT >= 32 ? 4 : 8);
+  constexpr int ROWS0 = NT >= 128 ? 2 : (NT >= 32 ? 4 : (NT >= 16 ? 8 : 16));
   constexpr int ROWS1 = ROWS0 * NT >= 32 ? ROWS0 : (32 + NT - 1) / NT;
   // static shared memory (ROWS rows of the padded transform) stays under 40 KB
   constexpr int ROWS = ROWS1 * (IdxPad16::pad(WH) + 2) * 8 <= 40960 ? ROWS1 : 1;
@@ -59,8 +59,9 @@ static int pad_rfft_t(const float* proj, const double* rowstats, int h, int norm
     if (cudaGetLastError() != cudaSuccess) return LGB_ERR_CUDA;
   }
   dim3 grid(ctas, n_c);
-  pad_rfft_kernel<WH, ROWS><<<grid, ROWS * NT, 0, s>>>(proj, rowstats, h, norm_h, norm_w, Wcp, ready,
-                                                       static_cast<float2*>(A));
+  // shared twiddle tables where a CTA transforms >= 4 rows
+  pad_rfft_kernel<WH, ROWS, (ROWS >= 4)><<<grid, ROWS * NT, 0, s>>>(proj, rowstats, h, norm_h, norm_w, Wcp, ready,
+                                                                    static_cast<float2*>(A));
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
