@@ -221,9 +221,11 @@ def precision_bench(args, dev):
     peaks, _ = _peaks()
     modes = [("fp32_b8", "fp32", 8), ("fp32_b32", "fp32", 32), ("bf16x3_b32", "bf16x3", 32),
              ("fp16x3_b32", "fp16x3", 32)]
+    graphs = {"fp32_b8_graph": ("fp32", 8, 32), "fp32_b32_graph": ("fp32", 32, 8)}
     out = {}
-    for label, prec, B in modes:
-        s = MatchTemplateSearch(**kw, device=dev, orientation_batch_size=B, precision=prec)
+    for label, prec, B in modes + [(k, v[0], v[1]) for k, v in graphs.items()]:
+        gb = graphs[label][2] if label in graphs else 0
+        s = MatchTemplateSearch(**kw, device=dev, orientation_batch_size=B, precision=prec, graph_batches=gb)
         s.run(0, N)  # warm-up: the whole grid once
         reps = 5
         a = torch.cuda.Event(enable_timing=True)
@@ -239,6 +241,7 @@ def precision_bench(args, dev):
             s.run(0, N)
             torch.cuda.synchronize(dev)
         entry = {"orientations_per_s": N / (ms / 1e3), "ms_per_grid": ms, "orientation_batch": B,
+                 "graph_batches": gb,
                  "stage_ms": {k: round(v, 4) for k, v in prof.ms.items() if prof.launches[k]}}
         if prec != "fp32":
             wq = -(-(W // 2 + 1) // 32) * 32
@@ -266,7 +269,7 @@ def precision_bench(args, dev):
     mip_r = ref["mip"].double()
     scale = mip_r.abs().clamp_min(1.0)
     sep = (mip_r - ref["second_best"].double()) > 1e-3 * scale
-    for label, prec, B in modes:
+    for label, prec, B in modes:  # graph replay changes no value: errors as without
         s = MatchTemplateSearch(**sub, device=dev, orientation_batch_size=B, precision=prec)
         s.run()
         res = s.result(to_cpu=True)
