@@ -336,6 +336,13 @@ int lgb_peaks_find(int H, int W, const float* zscore, float cutoff, float radius
  * D (device, FP32, row stride ldd) receives rows < m_valid, columns < n_valid.
  * Device pointers 16-byte aligned.  *err (device int) is set to
  * LGB_ERR_DEVICE_TIMEOUT if a bounded device wait ran out. */
+/* Self-test of the bounded device waits: one thread polls an mbarrier phase
+ * that never completes at most `polls` times (<= 2^22) and then writes
+ * LGB_ERR_DEVICE_TIMEOUT to *device_status -- the same expiry path as the
+ * waits inside lgb_tc_gemm and lgb_match_search_precision.  No GPU fault, no
+ * trap; the context stays usable. */
+int lgb_wait_timeout_selftest(unsigned polls, int* device_status, void* stream);
+
 int lgb_tc_gemm(int m_tiles, int n_tiles, int k_chunks, int bn, int f16, int terms, const void* a_hi,
                 const void* a_lo, const void* b_hi, const void* b_lo, float* d, int ldd, int m_valid, int n_valid,
                 int* err, void* stream);

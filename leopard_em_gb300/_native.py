@@ -110,6 +110,7 @@ _SIGNATURES = {
     "lgb_peaks_scratch_size": ([_I, _I, _I], _SZ),
     "lgb_peaks_find": ([_I, _I, _P, ctypes.c_float, ctypes.c_float, _I, _P, _SZ, _I, _P,
                         ctypes.POINTER(_I), ctypes.POINTER(_I), _P], _I),
+    "lgb_wait_timeout_selftest": ([ctypes.c_uint, _P, _P], _I),
     "lgb_tc_gemm": ([_I] * 6 + [_P] * 5 + [_I, _I, _I, _P, _P], _I),
     "lgb_nn_conv3x3_forward": ([_I] * 7 + [_P] * 4 + [_P], _I),
     "lgb_nn_conv3x3_backward": ([_I] * 6 + [_P] * 6 + [_P], _I),

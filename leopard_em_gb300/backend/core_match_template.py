@@ -293,6 +293,30 @@ class MatchTemplateSearch:
         return {"mip": self.mip, "best_global_index": self.best_index, "correlation_sum": self.corr_sum,
                 "correlation_squared_sum": self.corr_sq_sum}
 
+    def state_dict(self) -> dict:
+        """Resumable state (CPU tensors): the four maps and the orientations
+        folded so far.  The maps at a batch boundary plus the next orientation
+        index are a complete state of the search (the reference has no resume;
+        match_template_result.py:51-56 lists it as future work)."""
+        p = self.problem
+        return {
+            "maps": {k: v.cpu() for k, v in self.maps().items()},
+            "orientations_done": int(self.orientations_done),
+            "problem": {name: int(getattr(p, name)) for name, _ in p._fields_ if name != "col_waves"},
+        }
+
+    def load_state_dict(self, state: dict) -> None:
+        """Restore a ``state_dict`` taken from a search of the same shape."""
+        p = self.problem
+        mine = {name: int(getattr(p, name)) for name, _ in p._fields_ if name != "col_waves"}
+        mine.pop("orientation_batch")
+        theirs = dict(state["problem"])
+        theirs.pop("orientation_batch", None)
+        if mine != theirs:
+            raise ValueError(f"state of a different search shape: {theirs} vs {mine}")
+        self.load_maps(state["maps"])
+        self.orientations_done = int(state["orientations_done"])
+
     def load_maps(self, maps: dict) -> None:
         """Replace the running maps, e.g. with the reduction of every rank's maps."""
         with torch.cuda.device(self.device):

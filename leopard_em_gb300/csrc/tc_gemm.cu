@@ -33,9 +33,27 @@ static int tc_gemm_t(int m_tiles, int n_tiles, const TcGemmArgs& g, const EpiSto
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
+// Wait-timeout self-test: one thread waits on an mbarrier phase that nothing
+// completes, with a bounded number of polls, and reports the timeout through
+// the device status word -- the path every bounded wait takes on expiry.
+__global__ void wait_timeout_selftest_kernel(unsigned polls, int* status) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (!mbar_wait(&bar, 0, polls)) atomicExch(status, LGB_ERR_DEVICE_TIMEOUT);
+  }
+}
+
 }  // namespace lgb
 
 using namespace lgb;
+
+extern "C" int lgb_wait_timeout_selftest(unsigned polls, int* device_status, void* stream) {
+  if (!device_status || polls == 0 || polls > kTcSpinLimit) return LGB_ERR_INVALID_ARGUMENT;
+  wait_timeout_selftest_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(polls, device_status);
+  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+}
 
 extern "C" int lgb_tc_gemm(int m_tiles, int n_tiles, int k_chunks, int bn, int f16, int terms, const void* a_hi,
                            const void* a_lo, const void* b_hi, const void* b_lo, float* d, int ldd, int m_valid,
