@@ -95,7 +95,8 @@ def extract_peaks_and_statistics_zscore(mip, scaled_mip, best_psi, best_theta, b
         warnings.warn("No peaks found using z-score metric.", stacklevel=2)
 
     def at(t):
-        return torch.as_tensor(t)[pos_y.to(torch.as_tensor(t).device), pos_x.to(torch.as_tensor(t).device)]
+        t = torch.as_tensor(t)
+        return t[pos_y.to(t.device), pos_x.to(t.device)]
 
     return MatchTemplatePeaks(
         pos_y=pos_y, pos_x=pos_x, mip=at(mip), scaled_mip=at(scaled_mip), psi=at(best_psi), theta=at(best_theta),
