@@ -142,11 +142,11 @@ class BandpassFilterConfig:
     high_freq_cutoff: Optional[float] = None
     falloff: Optional[float] = None
 
-    def calculate_bandpass_filter(self, output_shape) -> torch.Tensor:
+    def calculate_bandpass_filter(self, output_shape, device=None) -> torch.Tensor:
         h, wc = output_shape
         if not self.enabled:
-            return torch.ones((h, wc), dtype=torch.float32)
-        ky, kx = pp.rfft_freq_grid((h, 2 * (wc - 1)))
+            return torch.ones((h, wc), dtype=torch.float32, device=device)
+        ky, kx = pp.rfft_freq_grid((h, 2 * (wc - 1)), device=device)
         r = torch.sqrt(kx**2 + ky**2)
         lo = self.low_freq_cutoff or 0.0
         hi = self.high_freq_cutoff if self.high_freq_cutoff is not None else 1.0
@@ -167,11 +167,12 @@ class PreprocessingFilters:
 
     def get_combined_filter(self, ref_img_rfft: torch.Tensor, output_shape) -> torch.Tensor:
         h, wc = output_shape
+        dev = ref_img_rfft.device
         if self.whitening_filter.enabled:
             wf = pp.whitening_filter(ref_img_rfft, (h, 2 * (wc - 1)))
         else:
-            wf = torch.ones((h, wc), dtype=torch.float32)
-        return wf * self.bandpass_filter.calculate_bandpass_filter(output_shape)
+            wf = torch.ones((h, wc), dtype=torch.float32, device=dev)
+        return wf * self.bandpass_filter.calculate_bandpass_filter(output_shape, device=dev)
 
 
 @dataclass
@@ -286,13 +287,18 @@ class MatchTemplateManager:
     micrograph_path: str = ""
     template_volume_path: str = ""
 
-    def make_backend_core_function_kwargs(self) -> dict:
-        """Backend inputs from held parameters (match_template_manager.py:140-218)."""
-        image = torch.as_tensor(self.micrograph, dtype=torch.float32)
-        template = torch.as_tensor(self.template_volume, dtype=torch.float32)
+    def make_backend_core_function_kwargs(self, preprocess_device=None) -> dict:
+        """Backend inputs from held parameters (match_template_manager.py:140-218).
+
+        ``preprocess_device`` (e.g. "cuda:0") runs the image rfft, the
+        whitening and bandpass filters, the CTF stack and the template rfft
+        there instead of on the host; the returned tensors live on it."""
+        dev = torch.device(preprocess_device) if preprocess_device is not None else torch.device("cpu")
+        image = torch.as_tensor(self.micrograph, dtype=torch.float32).to(dev)
+        template = torch.as_tensor(self.template_volume, dtype=torch.float32).to(dev)
         image_dft = torch.fft.rfftn(image)
         image_dft[0, 0] = 0 + 0j
-        bandpass = self.preprocessing_filters.bandpass_filter.calculate_bandpass_filter(image_dft.shape)
+        bandpass = self.preprocessing_filters.bandpass_filter.calculate_bandpass_filter(image_dft.shape, device=dev)
         cum_img = self.preprocessing_filters.get_combined_filter(image_dft, image_dft.shape)
         cum_tmp = self.preprocessing_filters.get_combined_filter(
             image_dft, (template.shape[-2], template.shape[-1] // 2 + 1))
@@ -305,7 +311,7 @@ class MatchTemplateManager:
                                   astigmatism_angle=og.astigmatism_angle, voltage=og.voltage,
                                   spherical_aberration=og.spherical_aberration,
                                   amplitude_contrast=og.amplitude_contrast_ratio, phase_shift=og.phase_shift,
-                                  pixel_size=og.pixel_size, b_factor=og.ctf_B_factor)
+                                  pixel_size=og.pixel_size, b_factor=og.ctf_B_factor, device=dev)
         return {
             "image_dft": image_pre.to(torch.complex64),
             "template_dft": pp.volume_to_rfft_fourier_slice(template).to(torch.complex64),
@@ -320,8 +326,9 @@ class MatchTemplateManager:
 
     def run_match_template(self, orientation_batch_size: int = 16, do_result_export: bool = True,
                            do_valid_cropping: bool = True) -> None:
-        """Run the search and populate ``match_template_result`` (:220-255, :327-358)."""
-        kw = self.make_backend_core_function_kwargs()
+        """Run the search and populate ``match_template_result`` (:220-255, :327-358).
+        Pre-processing runs on the search's GPU."""
+        kw = self.make_backend_core_function_kwargs(preprocess_device=self.computational_config.gpu_devices[0])
         res = core_match_template(**kw, orientation_batch_size=orientation_batch_size,
                                   num_cuda_streams=self.computational_config.num_cpus,
                                   backend=self.computational_config.backend)

@@ -1,4 +1,5 @@
-"""Host-side preparation of the search inputs (CPU torch, once per micrograph).
+"""Preparation of the search inputs (torch, once per micrograph, on the
+device of the tensors passed in: the GPU when the manager is given one).
 
 These mirror what ``MatchTemplateManager.make_backend_core_function_kwargs``
 does before calling the backend (match_template_manager.py:140-218):
@@ -9,7 +10,8 @@ does before calling the backend (match_template_manager.py:140-218):
   * ``get_cs_range``                  utils/search_utils.py:6-29
   * ``whitening_filter``              a radially averaged 1/sqrt(power) filter,
     the published construction of torch-fourier-filter's whitening_filter.
-They are not part of the timed search.
+They are not part of the timed search.  Every function works on the device
+of its input tensors (CPU or CUDA).
 """
 
 from __future__ import annotations
@@ -42,11 +44,11 @@ def preprocess_image(image_rfft, cumulative_fourier_filters, bandpass_filter, fu
     return image_rfft * ((img_h * img_w) / (box_h * box_w)) ** 0.5
 
 
-def rfft_freq_grid(shape: tuple[int, int], pixel_size: float = 1.0):
+def rfft_freq_grid(shape: tuple[int, int], pixel_size: float = 1.0, device=None):
     """(ky, kx) spatial frequencies (1/Angstrom) of an unshifted rfft grid."""
     h, w = shape
-    ky = torch.fft.fftfreq(h, dtype=torch.float64)[:, None] / pixel_size
-    kx = torch.fft.rfftfreq(w, dtype=torch.float64)[None, :] / pixel_size
+    ky = torch.fft.fftfreq(h, dtype=torch.float64, device=device)[:, None] / pixel_size
+    kx = torch.fft.rfftfreq(w, dtype=torch.float64, device=device)[None, :] / pixel_size
     return ky.expand(h, w // 2 + 1), kx.expand(h, w // 2 + 1)
 
 
@@ -68,6 +70,7 @@ def ctf_2d(
     phase_shift: float = 0.0,
     pixel_size: float = 1.0,
     b_factor: float = 0.0,
+    device=None,
 ) -> torch.Tensor:
     """CTF on an unshifted rfft grid: -sin(chi), defocus/astigmatism in Angstrom.
 
@@ -76,7 +79,7 @@ def ctf_2d(
     sign convention -sin(-pi lambda df k^2 + pi/2 Cs lambda^3 k^4 - phi - atan(A/sqrt(1-A^2))),
     and an optional B-factor envelope exp(-B k^2 / 4).
     """
-    ky, kx = rfft_freq_grid(shape, pixel_size)
+    ky, kx = rfft_freq_grid(shape, pixel_size, device)
     k2 = kx**2 + ky**2
     lam = electron_wavelength(voltage)
     cs = spherical_aberration * 1e7
@@ -108,6 +111,7 @@ def ctf_filter_stack(
     phase_shift: float = 0.0,
     pixel_size: float = 1.0,
     b_factor: float = 0.0,
+    device=None,
 ) -> torch.Tensor:
     """(num_pixel_sizes, num_defocus, d, d//2+1) stack as ctf_utils.py:19-116."""
     mean_df = (defocus_u + defocus_v) / 2
@@ -119,7 +123,7 @@ def ctf_filter_stack(
             torch.stack(
                 [
                     ctf_2d((template_size, template_size), mean_df + float(o), astig, astigmatism_angle, voltage, cs,
-                           amplitude_contrast, phase_shift, pixel_size, b_factor)
+                           amplitude_contrast, phase_shift, pixel_size, b_factor, device)
                     for o in defocus_offsets.tolist()
                 ]
             )
@@ -132,16 +136,19 @@ def whitening_filter(image_rfft: torch.Tensor, output_shape: tuple[int, int], nu
     (an rfft grid of real shape output_shape), normalised to max 1."""
     H = image_rfft.shape[-2]
     W = 2 * (image_rfft.shape[-1] - 1)
-    ky, kx = rfft_freq_grid((H, W))
+    dev = image_rfft.device
+    ky, kx = rfft_freq_grid((H, W), device=dev)
     r = torch.sqrt(kx**2 + ky**2)
     nb = num_bins or int(max(H, W) // 2 + 1)
     idx = torch.clamp((r / 0.5 * (nb - 1)).round().long(), 0, nb - 1)
-    power = torch.zeros(nb, dtype=torch.float64).index_add_(0, idx.flatten(), (image_rfft.abs() ** 2).flatten().double())
-    count = torch.zeros(nb, dtype=torch.float64).index_add_(0, idx.flatten(), torch.ones(idx.numel(), dtype=torch.float64))
+    power = torch.zeros(nb, dtype=torch.float64, device=dev).index_add_(
+        0, idx.flatten(), (image_rfft.abs() ** 2).flatten().double())
+    count = torch.zeros(nb, dtype=torch.float64, device=dev).index_add_(
+        0, idx.flatten(), torch.ones(idx.numel(), dtype=torch.float64, device=dev))
     spec = torch.sqrt(power / count.clamp_min(1))
     filt1d = torch.where(spec > 0, 1.0 / spec, torch.zeros_like(spec))
     filt1d = filt1d / filt1d.max()
-    ky2, kx2 = rfft_freq_grid(output_shape)
+    ky2, kx2 = rfft_freq_grid(output_shape, device=dev)
     r2 = torch.sqrt(kx2**2 + ky2**2)
     idx2 = torch.clamp((r2 / 0.5 * (nb - 1)).round().long(), 0, nb - 1)
     return filt1d[idx2].to(torch.float32)

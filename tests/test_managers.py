@@ -86,3 +86,21 @@ def test_refine_manager_runs_and_keeps_keys():
     res = mgr.run_refine_template(orientation_batch_size=16)
     assert set(res) >= {"refined_z_score", "refined_euler_angles", "refined_pos_y", "angle_idx"}
     assert res["refined_euler_angles"].shape == (2, 3)
+
+
+@pytest.mark.gpu
+def test_preprocessing_on_the_gpu_matches_the_host():
+    """make_backend_core_function_kwargs on the GPU gives the host's inputs."""
+    img = torch.randn(256, 288, generator=torch.Generator().manual_seed(2))
+    vol, _ = sy.blob_volume(32, 40, 1.5, 10.0, 0)
+    mgr = m.MatchTemplateManager(micrograph=img, template_volume=vol,
+                                 orientation_search_config=m.OrientationSearchConfig(psi_step=60, theta_step=60),
+                                 defocus_search_config=m.DefocusSearchConfig(defocus_min=-200, defocus_max=200,
+                                                                             defocus_step=200))
+    host = mgr.make_backend_core_function_kwargs()
+    dev = mgr.make_backend_core_function_kwargs(preprocess_device="cuda:0")
+    for k in ("image_dft", "template_dft", "ctf_filters", "whitening_filter_template"):
+        assert dev[k].is_cuda, k
+        a, b = host[k], dev[k].cpu()
+        assert a.shape == b.shape, k
+        assert (a - b).abs().max().item() <= 1e-4 * max(1.0, a.abs().max().item()), k
