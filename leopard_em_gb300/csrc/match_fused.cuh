@@ -285,7 +285,8 @@ struct RowFused {
   static constexpr int TAB = TableSize<1, RL>::value;
   static_assert(NBL % NT == 0, "last pass must give every thread whole butterflies");
   static_assert(NB1 <= NT * PER1, "first pass coverage");
-  static size_t smem(int wcp) { return sizeof(float2) * (size_t)(2 * wcp + ZS + TAB + WH); }
+  static_assert(16 % (2 * R1) == 0, "pre-twiddle roots exp(i pi q / R1) come from the 16th roots");
+  static size_t smem(int wcp) { return sizeof(float2) * (size_t)(2 * wcp + ZS + TAB); }
 };
 
 template <int WH, int NT, class RL>
@@ -301,7 +302,6 @@ __global__ void __launch_bounds__(NT, 2)
   float2* xr1 = rsm + Wcp;
   float2* z = rsm + 2 * Wcp;
   float2* tab = z + RF::ZS;
-  float2* pre = tab + RF::TAB;  // c2r pre-twiddle exp(+i pi k / WH)
   const int y = blockIdx.x;
   const int t = threadIdx.x;
   const int n16 = Wcp / 2;  // 16-byte chunks per row
@@ -313,10 +313,14 @@ __global__ void __launch_bounds__(NT, 2)
     cp_async_commit();
   }
   FillTables<WH, 1, RL>::run(tab, t, NT);
-  for (int k = t; k < WH; k += NT) {
-    float s, c;
-    sincospif((float)k / (float)WH, &s, &c);
-    pre[k] = make_float2(c, s);
+  // c2r pre-twiddle exp(+i pi k / WH) at k = j + q*NB1 factors into
+  // exp(+i pi j / WH) (per thread, kept in registers) x exp(+i pi q / R1)
+  float2 prej[PER1];
+#pragma unroll
+  for (int p = 0; p < PER1; ++p) {
+    float sn, cs;
+    sincospif((float)(t + p * NT) / (float)WH, &sn, &cs);
+    prej[p] = make_float2(cs, sn);
   }
   const float2* tab_last = tab + TableSize<1, typename DropLast<RL>::type>::value;
 
@@ -360,7 +364,8 @@ __global__ void __launch_bounds__(NT, 2)
               b.y = 0.f;
             }
             b.y = -b.y;
-            const float2 xo = cmul(csub(a, b), pre[k]);
+            float2 xo = cmul(csub(a, b), prej[p]);
+            if (q) xo = cmulc(xo, kRootsFwd16[q * (16 / (2 * R1))]);
             v[p][q] = cadd(cadd(a, b), mul_i<1>(xo));
           }
           Dft<R1, +1>::run(v[p]);
