@@ -1,6 +1,6 @@
 """GPU parity of the fused CUDA search against the oracle and the golden vectors.
 
-Acceptance (the benchmark spec's tolerances, written here):
+Acceptance tolerances:
   * MIP within 1e-4 relative, relative to max(|MIP|, 1): correlograms are
     normalised to unit variance, so 1 is their scale where a small search
     leaves a MIP near zero (the oracle's own FP32-vs-FP64 gap is ~6e-5 there);
