@@ -140,6 +140,64 @@ struct Dft<16, DIR> {
   }
 };
 
+template <int DIR>
+struct Dft<9, DIR> {
+  // 3 x 3:  u_i = DFT3(x_i, x_{i+3}, x_{i+6});
+  //         y[q1 + 3 q2] = DFT3_i(u_i[q1] * w9^(i q1))[q2]
+  static __device__ __forceinline__ void run(float2* v) {
+    // w9^m = (cos(2 pi m/9), DIR sin(2 pi m/9)), m = 1, 2, 4
+    const float c1 = 0.76604444311897804f, s1 = 0.64278760968653933f;
+    const float c2 = 0.17364817766693035f, s2 = 0.98480775301220806f;
+    const float c4 = -0.93969262078590838f, s4 = 0.34202014332566873f;
+    auto tw = [](float2 a, float c, float s) {  // a * (c + DIR*i*s)
+      float ss = DIR > 0 ? s : -s;
+      return make_float2(a.x * c - a.y * ss, a.x * ss + a.y * c);
+    };
+    float2 u[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      u[i][0] = v[i];
+      u[i][1] = v[i + 3];
+      u[i][2] = v[i + 6];
+      Dft<3, DIR>::run(u[i]);
+    }
+    u[1][1] = tw(u[1][1], c1, s1);
+    u[1][2] = tw(u[1][2], c2, s2);
+    u[2][1] = tw(u[2][1], c2, s2);
+    u[2][2] = tw(u[2][2], c4, s4);
+#pragma unroll
+    for (int q1 = 0; q1 < 3; ++q1) {
+      float2 t[3] = {u[0][q1], u[1][q1], u[2][q1]};
+      Dft<3, DIR>::run(t);
+      v[q1] = t[0];
+      v[q1 + 3] = t[1];
+      v[q1 + 6] = t[2];
+    }
+  }
+};
+
+template <int DIR>
+struct Dft<18, DIR> {
+  // Prime-factor (Good-Thomas) 2 x 9, no twiddles: input n = (9 n1 + 2 n2) mod 18,
+  // output k = (9 k1 + 10 k2) mod 18 (CRT map: 9 = 1 mod 2, 10 = 1 mod 9).
+  static __device__ __forceinline__ void run(float2* v) {
+    float2 a[9], b[9];
+#pragma unroll
+    for (int n2 = 0; n2 < 9; ++n2) {
+      const float2 x0 = v[(2 * n2) % 18], x1 = v[(9 + 2 * n2) % 18];
+      a[n2] = cadd(x0, x1);
+      b[n2] = csub(x0, x1);
+    }
+    Dft<9, DIR>::run(a);
+    Dft<9, DIR>::run(b);
+#pragma unroll
+    for (int k2 = 0; k2 < 9; ++k2) {
+      v[(10 * k2) % 18] = a[k2];
+      v[(9 + 10 * k2) % 18] = b[k2];
+    }
+  }
+};
+
 // ---------------------------------------------------------------------------
 // Twiddles w^t, t = 1..R-1, w = exp(DIR*2*pi*i*k/L)
 // ---------------------------------------------------------------------------

@@ -68,6 +68,22 @@ static int colpass_fused_t(const void* A, const void* Ip, int h, int Wcp, int n_
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
+template <int R1, int R2>
+static int colpass_pair_t(const void* A, const void* Ip, int h, int Wcp, int n_c, int cpi, int y_rows, int waves,
+                          void* Y, cudaStream_t s) {
+  using CP = ColPair<R1, R2>;
+  if (cudaFuncSetAttribute(colpass_pair_kernel<R1, R2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CP::SMEM) !=
+      cudaSuccess)
+    return LGB_ERR_CUDA;
+  int per = 1;
+  const int groups = (Wcp + CP::G - 1) / CP::G;
+  const int split = colpass_split(groups, n_c, waves, &per);
+  colpass_pair_kernel<R1, R2><<<dim3(groups, split), CP::THREADS, CP::SMEM, s>>>(
+      static_cast<const float2*>(A), static_cast<const float2*>(Ip), h, Wcp, n_c, per, cpi, y_rows,
+      static_cast<float2*>(Y));
+  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+}
+
 int launch_colpass(int H, const void* A, const void* Ip, int h, int Wcp, int n_c, int cpi, int y_rows, int waves,
                    void* Y, cudaStream_t s) {
   if (cpi < 1 || y_rows < 1 || y_rows > H || Wcp % kColGroup) return LGB_ERR_INVALID_ARGUMENT;
@@ -80,6 +96,8 @@ int launch_colpass(int H, const void* A, const void* Ip, int h, int Wcp, int n_c
       return colpass_fused_t<16, 2>(A, Ip, h, Wcp, n_c, cpi, y_rows, waves, Y, s);
     case 64:
       return colpass_fused_t<8, 2>(A, Ip, h, Wcp, n_c, cpi, y_rows, waves, Y, s);
+    case 288:
+      return colpass_pair_t<16, 18>(A, Ip, h, Wcp, n_c, cpi, y_rows, waves, Y, s);
     default:
       break;
   }

@@ -271,6 +271,106 @@ __global__ void __launch_bounds__(ColTab<HN>::G* ColTab<HN>::NT, ColTab<HN>::MIN
 }
 
 // ---------------------------------------------------------------------------
+// Column pass for H = R1*R2 (288 = 16*18) in two register passes per
+// direction.  Forward (Stockham): radix R1 over rows b + R2*q (pruned to the h
+// non-zero rows, read from global) -> shared transpose M1[b][q] -> radix R2
+// with twiddles w^(r*b), which leaves P[b + R1*r] in thread b; the cross
+// power and the inverse's first pass (radix R2, stride 1: the same elements)
+// stay in registers -> shared transpose M2[b][r] -> inverse radix R1 with
+// twiddles w^(-q*b) -> rows b + R2*q to global.  Two shared round trips per
+// column and correlogram; twiddle roots exp(-2 pi i m / H) for m = r*b <=
+// (R1-1)(R2-1) from one shared table.  Odd transpose row strides and a column
+// stride of 2 (mod 16) float2 make both transposes conflict free for the
+// lane layout (8 columns x consecutive butterflies).
+// ---------------------------------------------------------------------------
+template <int R1, int R2>
+struct ColPair {
+  static constexpr int N = R1 * R2;
+  static constexpr int NT = R1 > R2 ? R1 : R2;  // threads per column
+  static constexpr int G = 8;                   // columns per CTA: 64 B row segments
+  static constexpr int THREADS = G * NT;
+  static constexpr int S1 = R1 + 1, S2 = R2 + 1;  // transpose row strides
+  static_assert(S1 % 2 == 1 && S2 % 2 == 1, "odd transpose strides");
+  static constexpr int CB = R2 * S1 > R1 * S2 ? R2 * S1 : R1 * S2;
+  static constexpr int STRIDE = CB + (18 - CB % 16) % 16;  // = 2 (mod 16)
+  static constexpr int NROOT = (R1 - 1) * (R2 - 1) + 1;
+  static constexpr size_t SMEM = sizeof(float2) * ((size_t)G * STRIDE + NROOT);
+};
+
+template <int R1, int R2>
+__global__ void __launch_bounds__(ColPair<R1, R2>::THREADS, 4)
+    colpass_pair_kernel(const float2* __restrict__ A, const float2* __restrict__ Ip, int h, int Wcp, int n_c,
+                        int c_per_block, int c_per_image, int y_rows, float2* __restrict__ Y) {
+  using CP = ColPair<R1, R2>;
+  constexpr int N = CP::N, G = CP::G, S1 = CP::S1, S2 = CP::S2;
+  extern __shared__ float2 psm[];
+  float2* root = psm + G * CP::STRIDE;  // root[m] = exp(-2 pi i m / N)
+  for (int m = threadIdx.x; m < CP::NROOT; m += CP::THREADS) {
+    float sn, cs;
+    sincospif(2.0f * (float)m / (float)N, &sn, &cs);
+    root[m] = make_float2(cs, -sn);
+  }
+  const int g = threadIdx.x % G, b = threadIdx.x / G;
+  const int kx = blockIdx.x * G + g;
+  const bool col_ok = kx < Wcp;  // the last group may run past Wcp
+  float2* x = psm + g * CP::STRIDE;
+  const int c_begin = blockIdx.y * c_per_block;
+  const int c_end = min(n_c, c_begin + c_per_block);
+  __syncthreads();
+#pragma unroll 1
+  for (int c = c_begin; c < c_end; ++c) {
+    // ---- forward pass 1 (radix R1, stride 1): rows b + R2*q, rows >= h are zero
+    if (b < R2) {
+      float2 v[R1];
+      const float2* a = A + ((size_t)c * h + b) * Wcp + kx;
+#pragma unroll
+      for (int q = 0; q < R1; ++q)
+        v[q] = (col_ok && b + q * R2 < h) ? __ldg(a + (size_t)q * R2 * Wcp) : make_float2(0.f, 0.f);
+      Dft<R1, -1>::run(v);
+#pragma unroll
+      for (int q = 0; q < R1; ++q) x[b * S1 + q] = v[q];
+    }
+    __syncthreads();
+    float2 w[R2];
+    if (b < R1) {
+      // ---- forward pass 2 (radix R2, stride R1): w[r] = P[row b + R1*r]
+#pragma unroll
+      for (int r = 0; r < R2; ++r) w[r] = cmul(x[r * S1 + b], root[r * b]);
+      Dft<R2, -1>::run(w);
+      // ---- cross power with the image spectrum, P[0,0] = 0
+      const float2* ip = Ip + ((size_t)(c / c_per_image) * N + b) * Wcp + kx;
+#pragma unroll
+      for (int r = 0; r < R2; ++r) {
+        const float2 I = col_ok ? __ldg(ip + (size_t)r * R1 * Wcp) : make_float2(0.f, 0.f);
+        w[r] = (r == 0 && b == 0 && kx == 0) ? make_float2(0.f, 0.f) : cmulc(I, w[r]);
+      }
+      // ---- inverse pass 1 (radix R2, stride 1) on the same elements
+      Dft<R2, +1>::run(w);
+    }
+    __syncthreads();  // every read of M1 is done
+    if (b < R1) {
+#pragma unroll
+      for (int r = 0; r < R2; ++r) x[b * S2 + r] = w[r];
+    }
+    __syncthreads();
+    // ---- inverse pass 2 (radix R1, stride R2) -> rows b + R2*q
+    if (b < R2) {
+      float2 v[R1];
+#pragma unroll
+      for (int q = 0; q < R1; ++q) v[q] = cmulc(x[q * S2 + b], root[q * b]);
+      Dft<R1, +1>::run(v);
+      if (col_ok) {
+        float2* yo = Y + ((size_t)c * y_rows + b) * Wcp + kx;
+#pragma unroll
+        for (int q = 0; q < R1; ++q)
+          if (b + q * R2 < y_rows) yo[(size_t)q * R2 * Wcp] = v[q];
+      }
+    }
+    __syncthreads();  // before the next correlogram's pass-1 stores
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Fused row pass (c2r of length 2*WH + statistics).
 // ---------------------------------------------------------------------------
 template <int WH, int NT, class RL>
