@@ -363,8 +363,16 @@ def refine_plain_only(args):
     refine_particles_device(**dkw, device=dev, batch_size=cfg.batch)
     e1.record(stream)
     torch.cuda.synchronize(dev)
-    return {"metric": "refined particles/s (plain local grid)", "value": n / (e0.elapsed_time(e1) / 1e3),
-            "unit": "particles/s", "particles": n, "workload": cfg.name}
+    out = {"metric": "refined particles/s (plain local grid)", "value": n / (e0.elapsed_time(e1) / 1e3),
+           "unit": "particles/s", "particles": n, "workload": cfg.name}
+    # a second, separately timed pass with the per-stage events on
+    from leopard_em_gb300._native import StageProfile
+
+    with StageProfile() as prof:
+        refine_particles_device(**dkw, device=dev, batch_size=cfg.batch)
+        torch.cuda.synchronize(dev)
+    out["stage_ms_per_launch"] = {k: round(prof.ms[k] / prof.launches[k], 4) for k in prof.ms if prof.launches[k]}
+    return out
 
 
 def refine_bench(args, dev, with_cpu):

@@ -132,7 +132,7 @@ STAGE_NAMES = ("slice", "proj_col", "proj_row", "pad_rfft", "colpass", "rowpass"
 
 class StageProfile:
     """Context manager: per-stage device time (ms) and launch counts of every
-    lgb_match_search call made inside the ``with`` block."""
+    search or refinement call made inside the ``with`` block."""
 
     def __enter__(self):
         check(lib().lgb_profile_begin(), "lgb_profile_begin")

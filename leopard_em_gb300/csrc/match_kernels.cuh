@@ -84,6 +84,75 @@ __global__ void __launch_bounds__(COLS* FftThreads<HT>::value)
   }
 }
 
+// proj_col for HT = R1*R2 (256 = 16*16) in two register passes: radix R1
+// over rows t + R2*q of slice x filter straight from global memory ->
+// shared transpose M1[t][q] (odd stride R1+1; column stride 2 mod 16) ->
+// radix R2 with twiddles w^(r*t), w = exp(+2 pi i / HT) -> rows t + R1*r of T.
+// G columns per CTA (lane bits 0-2), one thread per butterfly.
+template <int R1, int R2>
+struct ProjColPair {
+  static constexpr int HT = R1 * R2;
+  static constexpr int NT = R1 > R2 ? R1 : R2;
+  static constexpr int G = 8;
+  static constexpr int S1 = R1 + 1;
+  static constexpr int CB = R2 * S1;
+  static constexpr int STRIDE = CB + (18 - CB % 16) % 16;  // = 2 (mod 16)
+  static constexpr int NROOT = (R1 - 1) * (R2 - 1) + 1;
+};
+
+template <int R1, int R2>
+__global__ void __launch_bounds__(ProjColPair<R1, R2>::G* ProjColPair<R1, R2>::NT)
+    proj_col_pair_kernel(const float2* __restrict__ slices, const float* __restrict__ pf, int nb, int n_cd,
+                         float2* __restrict__ T) {
+  using PC = ProjColPair<R1, R2>;
+  constexpr int HT = PC::HT, WC = HT / 2 + 1, G = PC::G, S1 = PC::S1;
+  __shared__ float2 buf[G * PC::STRIDE];
+  __shared__ float2 root[PC::NROOT];  // exp(+2 pi i m / HT)
+  for (int m = threadIdx.x; m < PC::NROOT; m += blockDim.x) {
+    float sn, cs;
+    sincospif(2.0f * (float)m / (float)HT, &sn, &cs);
+    root[m] = make_float2(cs, sn);
+  }
+  // c = (p*n_cd + cd)*nb + b: slices are per (p, b), filters per (p, cd)
+  const int c = blockIdx.y;
+  const int pc = c / nb, b = c - (c / nb) * nb;
+  const int p = pc / n_cd;
+  const float2* sl = slices + ((size_t)p * nb + b) * HT * WC;
+  const float* f = pf + (size_t)pc * HT * WC;
+  const int g = threadIdx.x % G, t = threadIdx.x / G;
+  const int kx = blockIdx.x * G + g;
+  const bool col_ok = kx < WC;
+  float2* x = buf + g * PC::STRIDE;
+  if (t < R2) {
+    float2 v[R1];
+#pragma unroll
+    for (int q = 0; q < R1; ++q) {
+      const int y = t + q * R2;
+      v[q] = make_float2(0.f, 0.f);
+      if (col_ok) {
+        const float2 s = __ldg(sl + (size_t)y * WC + kx);
+        const float w = __ldg(f + (size_t)y * WC + kx);
+        v[q] = make_float2(s.x * w, s.y * w);
+      }
+    }
+    Dft<R1, +1>::run(v);
+#pragma unroll
+    for (int q = 0; q < R1; ++q) x[t * S1 + q] = v[q];
+  }
+  __syncthreads();
+  if (t < R1) {
+    float2 w[R2];
+#pragma unroll
+    for (int r = 0; r < R2; ++r) w[r] = cmul(x[r * S1 + t], root[r * t]);
+    Dft<R2, +1>::run(w);
+    if (col_ok) {
+      float2* out = T + (size_t)c * HT * WC + (size_t)t * WC + kx;
+#pragma unroll
+      for (int r = 0; r < R2; ++r) out[(size_t)r * R1 * WC] = w[r];
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // proj_row: c2r along x of each row of T[c] (length HT via an HT/2 complex
 // inverse FFT), scale 1/HT^2, ifftshift both axes, and per-row moments
@@ -99,7 +168,7 @@ __global__ void __launch_bounds__(ROWS* FftThreads<HT / 2>::value)
   constexpr int ZS = IdxPad16::pad(M) + 2;
   __shared__ float2 xin[ROWS][WC];
   __shared__ float2 z[ROWS][ZS];
-  __shared__ double part[ROWS * NT][3];
+  __shared__ float part[ROWS * NT][3];
   const int c = blockIdx.y;
   const int g = threadIdx.x / NT, t = threadIdx.x - (threadIdx.x / NT) * NT;
   const int row0 = blockIdx.x * ROWS;
@@ -123,9 +192,10 @@ __global__ void __launch_bounds__(ROWS* FftThreads<HT / 2>::value)
   const int py = (y + HT - HT / 2) % HT;
   const float scale = 1.0f / ((float)HT * (float)HT);
   const bool edge_row = (py == 0) || (py == HT - 1);
-  // per-thread partial moments of <= M/NT pixel pairs in FP32 (FP64 arithmetic
-  // is a small fraction of the FP32 rate on this GPU); the cross-thread and
-  // cross-row reductions are FP64
+  // partial moments in FP32, per thread and then across the row's threads;
+  // FP64 only for the stored row moments (FP64 arithmetic, conversions
+  // included, runs at about one operation per SM per clock on this GPU); the
+  // cross-row reduction is FP64
   float s1 = 0.f, s2 = 0.f, se = 0.f;
   float* prow = proj + ((size_t)c * HT + py) * HT;
   for (int m = t; m < M; m += NT) {
@@ -143,21 +213,123 @@ __global__ void __launch_bounds__(ROWS* FftThreads<HT / 2>::value)
       if (px1 == 0 || px1 == HT - 1) se += b;
     }
   }
-  part[threadIdx.x][0] = (double)s1;
-  part[threadIdx.x][1] = (double)s2;
-  part[threadIdx.x][2] = (double)se;
+  part[threadIdx.x][0] = s1;
+  part[threadIdx.x][1] = s2;
+  part[threadIdx.x][2] = se;
   __syncthreads();
   if (t == 0) {
-    double a = 0, b = 0, e = 0;
+    float a = 0.f, b = 0.f, e = 0.f;
     for (int i = 0; i < NT; ++i) {
       a += part[g * NT + i][0];
       b += part[g * NT + i][1];
       e += part[g * NT + i][2];
     }
     double* rs = rowstats + ((size_t)c * HT + py) * 3;
-    rs[0] = a;
-    rs[1] = b;
-    rs[2] = e;
+    rs[0] = (double)a;
+    rs[1] = (double)b;
+    rs[2] = (double)e;
+  }
+}
+
+// proj_row for HT/2 = R1*R2 (128 = 16*8) in two register passes: the c2r
+// pre-twiddle is applied while loading the radix-R1 inputs k = t + R2*q from
+// the staged row; shared transpose M1[t][q]; radix R2 with twiddles w^(r*t)
+// leaves pixel pairs m = t + R1*r in thread t.  Same outputs, ifftshift and
+// moments as proj_row_kernel; R1 threads per row, ROWS rows per CTA.
+template <int R1, int R2, int ROWS>
+struct ProjRowPair {
+  static constexpr int M = R1 * R2;
+  static constexpr int NT = R1;
+  static constexpr int S1 = R1 + 1;
+  static constexpr int ZR = R2 * S1 + 1;
+  static constexpr int NROOT = (R1 - 1) * (R2 - 1) + 1;
+  static_assert(R1 >= R2, "second pass uses every thread of the row");
+};
+
+template <int R1, int R2, int ROWS>
+__global__ void __launch_bounds__(ROWS* R1)
+    proj_row_pair_kernel(const float2* __restrict__ T, float* __restrict__ proj, double* __restrict__ rowstats) {
+  using PR = ProjRowPair<R1, R2, ROWS>;
+  constexpr int M = PR::M, HT = 2 * M, WC = M + 1, NT = PR::NT, S1 = PR::S1;
+  __shared__ float2 xin[ROWS][WC + 1];
+  __shared__ float2 zb[ROWS][PR::ZR];
+  __shared__ float2 pre[M];            // exp(+i pi k / M)
+  __shared__ float2 root[PR::NROOT];   // exp(+2 pi i m / M)
+  static_assert(32 % R1 == 0, "rows must be lane aligned for the shuffle reduction");
+  for (int k = threadIdx.x; k < M; k += blockDim.x) {
+    float sn, cs;
+    sincospif((float)k / (float)M, &sn, &cs);
+    pre[k] = make_float2(cs, sn);
+  }
+  for (int m = threadIdx.x; m < PR::NROOT; m += blockDim.x) {
+    float sn, cs;
+    sincospif(2.0f * (float)m / (float)M, &sn, &cs);
+    root[m] = make_float2(cs, sn);
+  }
+  const int c = blockIdx.y;
+  const int g = threadIdx.x / NT, t = threadIdx.x - (threadIdx.x / NT) * NT;
+  const int row0 = blockIdx.x * ROWS;
+  const float2* src = T + ((size_t)c * HT + row0) * WC;
+  for (int e = threadIdx.x; e < ROWS * WC; e += blockDim.x) xin[e / WC][e % WC] = src[e];
+  __syncthreads();
+  // ---- pass 1 (radix R1, stride 1) on the pre-twiddled z[k], k = t + R2*q
+  if (t < R2) {
+    float2 v[R1];
+#pragma unroll
+    for (int q = 0; q < R1; ++q) {
+      const int k = t + q * R2;
+      float2 A = xin[g][k];
+      float2 B = xin[g][M - k];
+      if (k == 0) { A.y = 0.f; B.y = 0.f; }  // DC and Nyquist: real parts only
+      B.y = -B.y;                            // conj
+      const float2 xo = cmul(csub(A, B), pre[k]);
+      v[q] = cadd(cadd(A, B), mul_i<1>(xo));
+    }
+    Dft<R1, +1>::run(v);
+#pragma unroll
+    for (int q = 0; q < R1; ++q) zb[g][t * S1 + q] = v[q];
+  }
+  __syncthreads();
+  // ---- pass 2 (radix R2, stride R1): w[r] = z[t + R1*r]
+  float2 w[R2];
+#pragma unroll
+  for (int r = 0; r < R2; ++r) w[r] = cmul(zb[g][r * S1 + t], root[r * t]);
+  Dft<R2, +1>::run(w);
+  const int y = row0 + g;
+  const int py = (y + HT - HT / 2) % HT;
+  const float scale = 1.0f / ((float)HT * (float)HT);
+  const bool edge_row = (py == 0) || (py == HT - 1);
+  float s1 = 0.f, s2 = 0.f, se = 0.f;
+  float* prow = proj + ((size_t)c * HT + py) * HT;
+#pragma unroll
+  for (int r = 0; r < R2; ++r) {
+    const int m = t + r * R1;
+    const float a = w[r].x * scale, b = w[r].y * scale;
+    const int px0 = (2 * m + HT - HT / 2) % HT;  // even: px0 + 1 does not wrap
+    *reinterpret_cast<float2*>(prow + px0) = make_float2(a, b);
+    s1 += a + b;
+    s2 = fmaf(a, a, fmaf(b, b, s2));
+    if (edge_row) {
+      se += a + b;
+    } else {
+      if (px0 == 0) se += a;
+      if (px0 + 1 == HT - 1) se += b;
+    }
+  }
+  // row reduction across the row's R1 lanes in FP32 (R1 divides 32, rows are
+  // lane aligned); FP64 only for the stored row moments: this GPU's FP64 pipe
+  // retires about one operation per SM per clock, conversions included
+#pragma unroll
+  for (int o = R1 / 2; o > 0; o >>= 1) {
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    se += __shfl_xor_sync(0xffffffffu, se, o);
+  }
+  if (t == 0) {
+    double* rs = rowstats + ((size_t)c * HT + py) * 3;
+    rs[0] = (double)s1;
+    rs[1] = (double)s2;
+    rs[2] = (double)se;
   }
 }
 

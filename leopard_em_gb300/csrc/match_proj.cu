@@ -92,6 +92,14 @@ constexpr int kProjRows = 8;
 template <int HT>
 static int proj_col_t(const void* slices, const float* pf, int nb, int n_cd, int n_c, void* T, cudaStream_t s) {
   constexpr int WC = HT / 2 + 1;
+  if constexpr (HT == 256) {
+    // two register passes (16 x 16), 8 columns per CTA
+    using PC = ProjColPair<16, 16>;
+    dim3 pgrid((WC + PC::G - 1) / PC::G, n_c);
+    proj_col_pair_kernel<16, 16><<<pgrid, PC::G * PC::NT, 0, s>>>(static_cast<const float2*>(slices), pf, nb, n_cd,
+                                                                  static_cast<float2*>(T));
+    return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+  }
   dim3 grid((WC + kProjCols - 1) / kProjCols, n_c);
   proj_col_kernel<HT, kProjCols><<<grid, kProjCols * FftThreads<HT>::value, 0, s>>>(
       static_cast<const float2*>(slices), pf, nb, n_cd, static_cast<float2*>(T));
@@ -102,6 +110,12 @@ template <int HT>
 static int proj_row_t(const void* T, int n_c, float* proj, double* rowstats, cudaStream_t s) {
   static_assert(HT % kProjRows == 0, "rows per CTA must divide the template size");
   dim3 grid(HT / kProjRows, n_c);
+  if constexpr (HT == 256) {
+    // two register passes (16 x 8) of the 128-point c2r, 16 threads per row
+    proj_row_pair_kernel<16, 8, kProjRows><<<grid, kProjRows * 16, 0, s>>>(static_cast<const float2*>(T), proj,
+                                                                           rowstats);
+    return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+  }
   proj_row_kernel<HT, kProjRows><<<grid, kProjRows * FftThreads<HT / 2>::value, 0, s>>>(
       static_cast<const float2*>(T), proj, rowstats);
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;

@@ -13,6 +13,7 @@
 // Reference: backend/core_refine_template.py:555-767, utils/ctf_utils.py:19-116.
 #include <math.h>
 
+#include "profiler.h"
 #include "match_kernels.cuh"
 #include "match_launch.h"
 
@@ -175,6 +176,108 @@ __global__ void __launch_bounds__(NT)
   }
 }
 
+// The same row pass for WH = R1*R2 (144 = 16*9) in two register passes, ROWS
+// correlograms of one crop row per CTA (R1 threads each): the c2r
+// pre-twiddle is applied while loading the radix-R1 inputs k = t + R2*q from
+// the staged row; shared transpose M1[t][q]; radix R2 with twiddles w^(r*t)
+// leaves pixel pairs m = t + R1*r in thread t.  Same keys and reduction as
+// refine_rowpass_kernel.
+template <int R1, int R2, int ROWS>
+__global__ void __launch_bounds__(ROWS* R1)
+    refine_rowpass_pair_kernel(const float2* __restrict__ Y, int y_rows, int Wcp, int n_cpp, int c_per_block,
+                               int crop_w, float scale, const float* __restrict__ corr_mean,
+                               const float* __restrict__ corr_std, int crop_h,
+                               unsigned long long* __restrict__ slot_key, unsigned* __restrict__ slot_cc) {
+  constexpr int WH = R1 * R2, NT = R1, S1 = R1 + 1, NROOT = (R1 - 1) * (R2 - 1) + 1;
+  static_assert(R1 >= R2, "second pass uses every thread of the row");
+  __shared__ float2 xr[ROWS][WH + 2];
+  __shared__ float2 zb[ROWS][R2 * S1 + 1];
+  __shared__ float2 pre[WH];      // exp(+i pi k / WH)
+  __shared__ float2 root[NROOT];  // exp(+2 pi i m / WH)
+  __shared__ unsigned long long red_key[1];
+  __shared__ unsigned red_cc[1];
+  for (int k = threadIdx.x; k < WH; k += blockDim.x) {
+    float sn, cs;
+    sincospif((float)k / (float)WH, &sn, &cs);
+    pre[k] = make_float2(cs, sn);
+  }
+  for (int m = threadIdx.x; m < NROOT; m += blockDim.x) {
+    float sn, cs;
+    sincospif(2.0f * (float)m / (float)WH, &sn, &cs);
+    root[m] = make_float2(cs, sn);
+  }
+  if (threadIdx.x == 0) {
+    red_key[0] = 0ull;
+    red_cc[0] = 0u;
+  }
+  const int y = blockIdx.x, p = blockIdx.y;
+  const int g = threadIdx.x / NT, t = threadIdx.x - (threadIdx.x / NT) * NT;
+  unsigned long long best_key = 0ull;
+  unsigned best_cc = 0u;
+  const float* mrow = corr_mean + ((size_t)p * crop_h + y) * crop_w;
+  const float* srow = corr_std + ((size_t)p * crop_h + y) * crop_w;
+  const int c_begin = blockIdx.z * c_per_block;
+  const int c_end = min(n_cpp, c_begin + c_per_block);
+  for (int cb = c_begin; cb < c_end; cb += ROWS) {
+    const int c = cb + g;
+    const bool act = c < c_end;
+    __syncthreads();  // tables filled / the previous rows fully read
+    if (act) {
+      const float2* row = Y + (((size_t)p * n_cpp + c) * y_rows + y) * Wcp;
+      for (int k = t; k <= WH; k += NT) xr[g][k] = row[k];
+    }
+    __syncthreads();
+    if (act && t < R2) {
+      float2 v[R1];
+#pragma unroll
+      for (int q = 0; q < R1; ++q) {
+        const int k = t + q * R2;
+        float2 A = xr[g][k];
+        float2 B = xr[g][WH - k];
+        if (k == 0) { A.y = 0.f; B.y = 0.f; }
+        B.y = -B.y;
+        const float2 xo = cmul(csub(A, B), pre[k]);
+        v[q] = cadd(cadd(A, B), mul_i<1>(xo));
+      }
+      Dft<R1, +1>::run(v);
+#pragma unroll
+      for (int q = 0; q < R1; ++q) zb[g][t * S1 + q] = v[q];
+    }
+    __syncthreads();
+    if (act) {
+      float2 w[R2];
+#pragma unroll
+      for (int r = 0; r < R2; ++r) w[r] = cmul(zb[g][r * S1 + t], root[r * t]);
+      Dft<R2, +1>::run(w);
+#pragma unroll
+      for (int r = 0; r < R2; ++r) {
+        const int m = t + r * R1;
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+          const int x = 2 * m + hh;
+          if (x < crop_w) {
+            const float cc = (hh ? w[r].y : w[r].x) * scale;
+            const float zz = (cc - mrow[x]) / srow[x];
+            const unsigned flat = (unsigned)((y * crop_w + x) * n_cpp + c);
+            const unsigned long long key = ((unsigned long long)ord_f(zz) << 32) | (unsigned long long)(~flat);
+            best_key = key > best_key ? key : best_key;
+            const unsigned oc = ord_f(cc);
+            best_cc = oc > best_cc ? oc : best_cc;
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  atomicMax(&red_key[0], best_key);
+  atomicMax(&red_cc[0], best_cc);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicMax(slot_key + p, red_key[0]);
+    atomicMax(slot_cc + p, red_cc[0]);
+  }
+}
+
 // Strict '>' update of each particle's best (core_refine_template.py:725),
 // then reset of the batch slots.
 __global__ void refine_commit_kernel(int P, unsigned long long* slot_key, unsigned* slot_cc, int o0, int nb,
@@ -227,6 +330,15 @@ template <int WH>
 static int refine_rowpass_t(const void* Y, int y_rows, int Wcp, int n_cpp, int P, int crop_h, int crop_w,
                             float scale, const float* mean, const float* std_, unsigned long long* key, unsigned* cc,
                             cudaStream_t s) {
+  if constexpr (WH == 144) {
+    // two register passes (16 x 9), 16 correlograms per step, two steps per CTA
+    constexpr int ROWS = 16;
+    const int per = 2 * ROWS;
+    dim3 grid(crop_h, P, (n_cpp + per - 1) / per);
+    refine_rowpass_pair_kernel<16, 9, ROWS><<<grid, ROWS * 16, 0, s>>>(
+        static_cast<const float2*>(Y), y_rows, Wcp, n_cpp, per, crop_w, scale, mean, std_, crop_h, key, cc);
+    return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+  }
   constexpr int NT = row_threads(WH);
   // split each particle's correlograms until the grid covers ~4 waves of the SMs
   int dev = 0, sms = 0;
@@ -393,6 +505,7 @@ int lgb_refine_search(const lgb_refine_problem* p, const lgb_ctf_params* ctf, co
                                                        best_batch_len, key, cc);
   if (cudaGetLastError() != cudaSuccess) return LGB_ERR_CUDA;
   const float scale = 1.0f / ((float)H * (float)W);
+  const bool prof = profiling_on();
   int st;
   for (int o0 = 0; o0 < p->n_offsets; o0 += p->offset_batch) {
     const int nb = (p->n_offsets - o0) < p->offset_batch ? (p->n_offsets - o0) : p->offset_batch;
@@ -400,14 +513,32 @@ int lgb_refine_search(const lgb_refine_problem* p, const lgb_ctf_params* ctf, co
     const int n_c = P * n_cpp;
     refine_rotations_kernel<<<(P * nb + 127) / 128, 128, 0, s>>>(euler_angles, euler_offsets, o0, nb, P, rot);
     if (cudaGetLastError() != cudaSuccess) return LGB_ERR_CUDA;
-    if ((st = launch_slice(template_dft, d, nullptr, 0, nullptr, P * nb, rot, slices, s))) return st;
-    if ((st = launch_proj_col(d, slices, filt, nb, L.n_cd, n_c, T, s))) return st;
-    if ((st = launch_proj_row(d, T, n_c, proj, rowstats, s))) return st;
-    if ((st = launch_pad_rfft(W, proj, rowstats, d, H, W, L.wcp, n_c, A, s))) return st;
-    if ((st = launch_colpass(H, A, ip, d, L.wcp, n_c, n_cpp, L.crop_h, 0, Y, s))) return st;
-    if ((st = launch_refine_rowpass(W, Y, L.crop_h, L.wcp, n_cpp, P, L.crop_h, L.crop_w, scale, corr_mean, corr_std,
-                                    key, cc, s)))
-      return st;
+    {
+      StageScope sc(LGB_STAGE_SLICE, s, prof);
+      if ((st = launch_slice(template_dft, d, nullptr, 0, nullptr, P * nb, rot, slices, s))) return st;
+    }
+    {
+      StageScope sc(LGB_STAGE_PROJ_COL, s, prof);
+      if ((st = launch_proj_col(d, slices, filt, nb, L.n_cd, n_c, T, s))) return st;
+    }
+    {
+      StageScope sc(LGB_STAGE_PROJ_ROW, s, prof);
+      if ((st = launch_proj_row(d, T, n_c, proj, rowstats, s))) return st;
+    }
+    {
+      StageScope sc(LGB_STAGE_PAD_RFFT, s, prof);
+      if ((st = launch_pad_rfft(W, proj, rowstats, d, H, W, L.wcp, n_c, A, s))) return st;
+    }
+    {
+      StageScope sc(LGB_STAGE_COLPASS, s, prof);
+      if ((st = launch_colpass(H, A, ip, d, L.wcp, n_c, n_cpp, L.crop_h, 0, Y, s))) return st;
+    }
+    {
+      StageScope sc(LGB_STAGE_ROWPASS, s, prof);
+      if ((st = launch_refine_rowpass(W, Y, L.crop_h, L.wcp, n_cpp, P, L.crop_h, L.crop_w, scale, corr_mean,
+                                      corr_std, key, cc, s)))
+        return st;
+    }
     refine_commit_kernel<<<(P + 127) / 128, 128, 0, s>>>(P, key, cc, o0, nb, best_z, best_cc, best_flat,
                                                            best_offset_begin, best_batch_len);
     if (cudaGetLastError() != cudaSuccess) return LGB_ERR_CUDA;
