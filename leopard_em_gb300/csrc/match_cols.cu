@@ -70,7 +70,7 @@ static int colpass_fused_t(const void* A, const void* Ip, int h, int Wcp, int n_
 
 template <int R1, int R2>
 static int colpass_pair_t(const void* A, const void* Ip, int h, int Wcp, int n_c, int cpi, int y_rows, int waves,
-                          void* Y, cudaStream_t s) {
+                          void* Y, cudaStream_t s, const float2* norm, int norm_stride, int norm_w) {
   using CP = ColPair<R1, R2>;
   if (cudaFuncSetAttribute(colpass_pair_kernel<R1, R2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CP::SMEM) !=
       cudaSuccess)
@@ -80,13 +80,14 @@ static int colpass_pair_t(const void* A, const void* Ip, int h, int Wcp, int n_c
   const int split = colpass_split(groups, n_c, waves, &per);
   colpass_pair_kernel<R1, R2><<<dim3(groups, split), CP::THREADS, CP::SMEM, s>>>(
       static_cast<const float2*>(A), static_cast<const float2*>(Ip), h, Wcp, n_c, per, cpi, y_rows,
-      static_cast<float2*>(Y));
+      static_cast<float2*>(Y), norm, norm_stride, norm_w);
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
 int launch_colpass(int H, const void* A, const void* Ip, int h, int Wcp, int n_c, int cpi, int y_rows, int waves,
-                   void* Y, cudaStream_t s) {
+                   void* Y, cudaStream_t s, const float2* norm, int norm_stride, int norm_w) {
   if (cpi < 1 || y_rows < 1 || y_rows > H || Wcp % kColGroup) return LGB_ERR_INVALID_ARGUMENT;
+  if (norm && (H != 288 || norm_w < 2 || norm_w / 2 + 1 > Wcp || norm_stride < 1)) return LGB_ERR_UNSUPPORTED_SIZE;
   switch (H) {
     case 4096:
       return colpass_fused_t<16, 3>(A, Ip, h, Wcp, n_c, cpi, y_rows, waves, Y, s);
@@ -97,7 +98,7 @@ int launch_colpass(int H, const void* A, const void* Ip, int h, int Wcp, int n_c
     case 64:
       return colpass_fused_t<8, 2>(A, Ip, h, Wcp, n_c, cpi, y_rows, waves, Y, s);
     case 288:
-      return colpass_pair_t<16, 18>(A, Ip, h, Wcp, n_c, cpi, y_rows, waves, Y, s);
+      return colpass_pair_t<16, 18>(A, Ip, h, Wcp, n_c, cpi, y_rows, waves, Y, s, norm, norm_stride, norm_w);
     default:
       break;
   }

@@ -300,7 +300,8 @@ struct ColPair {
 template <int R1, int R2>
 __global__ void __launch_bounds__(ColPair<R1, R2>::THREADS, 4)
     colpass_pair_kernel(const float2* __restrict__ A, const float2* __restrict__ Ip, int h, int Wcp, int n_c,
-                        int c_per_block, int c_per_image, int y_rows, float2* __restrict__ Y) {
+                        int c_per_block, int c_per_image, int y_rows, float2* __restrict__ Y,
+                        const float2* __restrict__ norm, int norm_stride, int norm_w) {
   using CP = ColPair<R1, R2>;
   constexpr int N = CP::N, G = CP::G, S1 = CP::S1, S2 = CP::S2;
   extern __shared__ float2 psm[];
@@ -316,6 +317,22 @@ __global__ void __launch_bounds__(ColPair<R1, R2>::THREADS, 4)
   float2* x = psm + g * CP::STRIDE;
   const int c_begin = blockIdx.y * c_per_block;
   const int c_end = min(n_c, c_begin + c_per_block);
+  // deferred normalisation: rfft_W((p - e) s) = s (A - e U), U[k] = sum_{x<h} w^(k x)
+  // = exp(-i pi k (h-1) / W) sin(pi k h / W) / sin(pi k / W), w = exp(-2 pi i / W)
+  float2 U = make_float2(0.f, 0.f);
+  if (norm && col_ok && kx <= norm_w / 2) {
+    if (kx == 0) {
+      U = make_float2((float)h, 0.f);
+    } else {
+      const int w2 = 2 * norm_w;
+      float sa, ca, sn, cn, sd, cd;
+      sincospif((float)((kx * (h - 1)) % w2) / (float)norm_w, &sa, &ca);
+      sincospif((float)((kx * h) % w2) / (float)norm_w, &sn, &cn);
+      sincospif((float)kx / (float)norm_w, &sd, &cd);
+      const float mag = sn / sd;
+      U = make_float2(ca * mag, -sa * mag);
+    }
+  }
   __syncthreads();
 #pragma unroll 1
   for (int c = c_begin; c < c_end; ++c) {
@@ -326,6 +343,13 @@ __global__ void __launch_bounds__(ColPair<R1, R2>::THREADS, 4)
 #pragma unroll
       for (int q = 0; q < R1; ++q)
         v[q] = (col_ok && b + q * R2 < h) ? __ldg(a + (size_t)q * R2 * Wcp) : make_float2(0.f, 0.f);
+      if (norm) {
+        const float2 es = __ldg(norm + (size_t)c * norm_stride);
+        const float2 eU = make_float2(es.x * U.x, es.x * U.y);
+#pragma unroll
+        for (int q = 0; q < R1; ++q)
+          if (b + q * R2 < h) v[q] = make_float2(es.y * (v[q].x - eU.x), es.y * (v[q].y - eU.y));
+      }
       Dft<R1, -1>::run(v);
 #pragma unroll
       for (int q = 0; q < R1; ++q) x[b * S1 + q] = v[q];

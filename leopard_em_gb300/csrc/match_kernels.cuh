@@ -333,6 +333,148 @@ __global__ void __launch_bounds__(ROWS* R1)
   }
 }
 
+// proj_row and the zero-padded row rfft in one kernel, for d = 256 templates
+// and rows of W = 288 (the refinement crops).  Per row y of T[c]: the 256-point
+// c2r as in proj_row_pair_kernel<16, 8> (pixel pairs m = t + 16r in thread t),
+// the row moments, the ifftshift (pair m -> m' = (m + 64) mod 128), then the
+// rfft of the un-normalised row zero padded to W in two register passes
+// (144 = 16 x 9) and the real post-process:
+//   A[c][py][k] = sum_{px < d} p[py][px] exp(-2 pi i k px / W),  k <= W/2.
+// The projection never goes to memory.  Its normalisation (p - e) s
+// (utils.py:106-188) is affine, rfft((p - e) s) = s (A - e U) with
+// U[k] = sum_{px < d} exp(-2 pi i k px / W), and is applied by the column pass.
+template <int ROWS>
+__global__ void __launch_bounds__(ROWS * 16)
+    proj_row_rfft_kernel(const float2* __restrict__ T, double* __restrict__ rowstats, int Wcp,
+                         float2* __restrict__ A) {
+  constexpr int HT = 256, M = 128, WC = M + 1, NT = 16, S1 = 17;
+  constexpr int WH = 144;  // W / 2
+  constexpr int C2 = 8;    // c2r: M = 16 x 8
+  constexpr int R2 = 9;    // rfft: WH = 16 x 9
+  constexpr int ZR = IdxPad16::pad(WH) + 2;
+  __shared__ float2 xin[ROWS][WC + 1];
+  __shared__ float2 zb[ROWS][R2 * S1 + 1];  // c2r transpose (8 x 17), then rfft transpose (9 x 17)
+  __shared__ float2 zr[ROWS][ZR];           // rfft input z[m'] (zero for m' >= 128), then Z
+  __shared__ float2 pre[M];                 // exp(+i pi k / M)
+  __shared__ float2 rootc[15 * (C2 - 1) + 1];  // exp(+2 pi i m / M)
+  __shared__ float2 rootr[15 * (R2 - 1) + 1];  // exp(-2 pi i m / WH)
+  __shared__ float2 post[WH + 1];              // exp(-i pi k / WH)
+  for (int k = threadIdx.x; k < M; k += blockDim.x) {
+    float sn, cs;
+    sincospif((float)k / (float)M, &sn, &cs);
+    pre[k] = make_float2(cs, sn);
+  }
+  for (int m = threadIdx.x; m < 15 * (C2 - 1) + 1; m += blockDim.x) {
+    float sn, cs;
+    sincospif(2.0f * (float)m / (float)M, &sn, &cs);
+    rootc[m] = make_float2(cs, sn);
+  }
+  for (int m = threadIdx.x; m < 15 * (R2 - 1) + 1; m += blockDim.x) {
+    float sn, cs;
+    sincospif(2.0f * (float)m / (float)WH, &sn, &cs);
+    rootr[m] = make_float2(cs, -sn);
+  }
+  for (int k = threadIdx.x; k <= WH; k += blockDim.x) {
+    float sn, cs;
+    sincospif((float)k / (float)WH, &sn, &cs);
+    post[k] = make_float2(cs, -sn);
+  }
+  const int c = blockIdx.y;
+  const int g = threadIdx.x / NT, t = threadIdx.x - (threadIdx.x / NT) * NT;
+  const int row0 = blockIdx.x * ROWS;
+  const float2* src = T + ((size_t)c * HT + row0) * WC;
+  for (int e = threadIdx.x; e < ROWS * WC; e += blockDim.x) xin[e / WC][e % WC] = src[e];
+  __syncthreads();
+  // ---- c2r pass 1 (radix 16) on the pre-twiddled z[k], k = t + 8q
+  if (t < C2) {
+    float2 v[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int k = t + q * C2;
+      float2 a = xin[g][k];
+      float2 b = xin[g][M - k];
+      if (k == 0) { a.y = 0.f; b.y = 0.f; }  // DC and Nyquist: real parts only
+      b.y = -b.y;
+      const float2 xo = cmul(csub(a, b), pre[k]);
+      v[q] = cadd(cadd(a, b), mul_i<1>(xo));
+    }
+    Dft<16, +1>::run(v);
+#pragma unroll
+    for (int q = 0; q < 16; ++q) zb[g][t * S1 + q] = v[q];
+  }
+  __syncthreads();
+  // ---- c2r pass 2 (radix 8): pixel pairs m = t + 16r, moments, shifted rfft input
+  const int y = row0 + g;
+  const int py = (y + HT - HT / 2) % HT;
+  {
+    float2 w[C2];
+#pragma unroll
+    for (int r = 0; r < C2; ++r) w[r] = cmul(zb[g][r * S1 + t], rootc[r * t]);
+    Dft<C2, +1>::run(w);
+    const float scale = 1.0f / ((float)HT * (float)HT);
+    const bool edge_row = (py == 0) || (py == HT - 1);
+    float s1 = 0.f, s2 = 0.f, se = 0.f;
+#pragma unroll
+    for (int r = 0; r < C2; ++r) {
+      const int m = t + r * 16;
+      const float a = w[r].x * scale, b = w[r].y * scale;
+      const int mp = (m + M / 2) & (M - 1);  // ifftshift: px = 2 mp, 2 mp + 1
+      zr[g][IdxPad16::f(mp)] = make_float2(a, b);
+      s1 += a + b;
+      s2 = fmaf(a, a, fmaf(b, b, s2));
+      if (edge_row) {
+        se += a + b;
+      } else {
+        if (mp == 0) se += a;
+        if (mp == M - 1) se += b;
+      }
+    }
+    zr[g][IdxPad16::f(M + t)] = make_float2(0.f, 0.f);  // zero padding m' = 128..143
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) {
+      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+      se += __shfl_xor_sync(0xffffffffu, se, o);
+    }
+    if (t == 0) {
+      double* rs = rowstats + ((size_t)c * HT + py) * 3;
+      rs[0] = (double)s1;
+      rs[1] = (double)s2;
+      rs[2] = (double)se;
+    }
+  }
+  __syncthreads();
+  // ---- rfft pass 1 (radix 16) over m' = t + 9q
+  if (t < R2) {
+    float2 v[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = zr[g][IdxPad16::f(t + q * R2)];
+    Dft<16, -1>::run(v);
+#pragma unroll
+    for (int q = 0; q < 16; ++q) zb[g][t * S1 + q] = v[q];
+  }
+  __syncthreads();
+  // ---- rfft pass 2 (radix 9): Z[t + 16r]
+  {
+    float2 u[R2];
+#pragma unroll
+    for (int r = 0; r < R2; ++r) u[r] = cmul(zb[g][r * S1 + t], rootr[r * t]);
+    Dft<R2, -1>::run(u);
+#pragma unroll
+    for (int r = 0; r < R2; ++r) zr[g][IdxPad16::f(t + 16 * r)] = u[r];
+  }
+  __syncthreads();
+  float2* out = A + ((size_t)c * HT + py) * Wcp;
+  for (int k = t; k <= WH; k += NT) {
+    const float2 Zk = zr[g][IdxPad16::f(k == WH ? 0 : k)];
+    const float2 Zm = cconj(zr[g][IdxPad16::f(k == 0 ? 0 : WH - k)]);
+    const float2 xe = cscale(cadd(Zk, Zm), 0.5f);
+    const float2 xo = mul_i<-1>(cscale(csub(Zk, Zm), 0.5f));
+    out[k] = cadd(xe, cmul(post[k], xo));
+  }
+  for (int k = WH + 1 + t; k < Wcp; k += NT) out[k] = make_float2(0.f, 0.f);
+}
+
 // Normalisation constants of utils.py:106-188 from the per-row moments:
 // returns edge mean e and scale s such that normalised = (p - e) * s.
 // Called by all 32 lanes of warp 0 (the launcher guarantees a full warp).
@@ -394,13 +536,14 @@ __global__ void __launch_bounds__(ROWS* FftThreads<WH>::value)
     }
   }
   const int c = blockIdx.y;
-  // norm_ready: constants precomputed by norm_constants_kernel in
-  // rowstats[c][0][0..1]; otherwise warp 0 reduces the row moments here
+  // norm_ready: constants (e, s) precomputed by norm_constants_kernel as a
+  // float2 over rowstats[c][0][0]; otherwise warp 0 reduces the row moments here
   __shared__ float norm[2];
   if (norm_ready) {
     if (threadIdx.x == 0) {
-      norm[0] = (float)rowstats[(size_t)c * h * 3];
-      norm[1] = (float)rowstats[(size_t)c * h * 3 + 1];
+      const float2 es = *reinterpret_cast<const float2*>(rowstats + (size_t)c * h * 3);
+      norm[0] = es.x;
+      norm[1] = es.y;
     }
   } else if (threadIdx.x < 32) {
     projection_norm_constants(rowstats + (size_t)c * h * 3, h, norm_h, norm_w, &norm[0], &norm[1]);

@@ -21,6 +21,14 @@ bool supported_refine_row(int W);
 // c = (p*n_cd + cd)*nb + b; slices [P][nb], filters [P][n_cd] (P = n_c / (n_cd*nb))
 int launch_proj_col(int h, const void* slices, const float* pf, int nb, int n_cd, int n_c, void* T, cudaStream_t s);
 int launch_proj_row(int h, const void* T, int n_c, float* proj, double* rowstats, cudaStream_t s);
+// proj_row and the zero-padded row rfft of the un-normalised projection in one
+// kernel (h = 256, W = 288 only): A[c][py][k] = rfft_W(p[py])[k], row moments
+// in rowstats.  The column pass then applies the normalisation (norm below).
+bool supported_proj_row_rfft(int h, int W);
+int launch_proj_row_rfft(int h, int W, const void* T, int n_c, double* rowstats, int Wcp, void* A, cudaStream_t s);
+// Per-correlogram normalisation constants (e, s) from the row moments, stored
+// as a float2 over rowstats[c][0][0].
+int launch_norm_constants(double* rowstats, int n_c, int h, int norm_h, int norm_w, cudaStream_t s);
 // Projections normalised for a norm_h x norm_w micrograph (utils.py:106-188),
 // rfft'd at length W (W >= norm_w: zero padding beyond the micrograph).
 int launch_pad_rfft(int W, const float* proj, const double* rowstats, int h, int norm_h, int norm_w, int Wcp,
@@ -29,8 +37,12 @@ int launch_pad_rfft(int W, const float* proj, const double* rowstats, int h, int
 // Only rows y < y_rows of each inverse column transform are stored (Y is [n_c][y_rows][Wcp]).
 // waves: the correlogram range is split until the grid covers about waves x
 // the SM count (0 = 4).
+// norm (H = 288 only; null otherwise): A holds un-normalised row spectra of
+// length norm_w rows and correlogram c is normalised on load as
+// s (A - e U[kx]), (e, s) = norm[c * norm_stride], U[k] = sum_{x < h} exp(-2 pi i k x / norm_w).
 int launch_colpass(int H, const void* A, const void* Ip, int h, int Wcp, int n_c, int c_per_image, int y_rows,
-                   int waves, void* Y, cudaStream_t s);
+                   int waves, void* Y, cudaStream_t s, const float2* norm = nullptr, int norm_stride = 0,
+                   int norm_w = 0);
 // Rows y < y_rows of the H x W correlograms (Y is [n_c][y_rows][Wcp]); global
 // index base o0 + *o0_dev (o0_dev may be null).
 int launch_rowpass(int W, const void* Y, int H, int y_rows, int Wcp, int n_c, int nb, int n_orient, int o0,

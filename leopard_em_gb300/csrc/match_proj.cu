@@ -121,6 +121,15 @@ static int proj_row_t(const void* T, int n_c, float* proj, double* rowstats, cud
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
+bool supported_proj_row_rfft(int h, int W) { return h == 256 && W == 288; }
+
+int launch_proj_row_rfft(int h, int W, const void* T, int n_c, double* rowstats, int Wcp, void* A, cudaStream_t s) {
+  if (!supported_proj_row_rfft(h, W) || Wcp < W / 2 + 1) return LGB_ERR_UNSUPPORTED_SIZE;
+  proj_row_rfft_kernel<kProjRows><<<dim3(256 / kProjRows, n_c), kProjRows * 16, 0, s>>>(
+      static_cast<const float2*>(T), rowstats, Wcp, static_cast<float2*>(A));
+  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+}
+
 int launch_proj_col(int h, const void* slices, const float* pf, int nb, int n_cd, int n_c, void* T, cudaStream_t s) {
   switch (h) {
 #define X(n) \

@@ -6,10 +6,10 @@
 
 namespace lgb {
 
-// One warp per correlogram: the normalisation constants (edge mean, scale)
-// from the h row moments, stored as two doubles over rowstats[c][0][0..1]
-// (row 0's moments are not needed afterwards), so that every pad_rfft CTA
-// reads them instead of reducing all rows again.
+// One warp per correlogram: the normalisation constants (edge mean e, scale
+// s) from the h row moments, stored as a float2 over rowstats[c][0][0] (row
+// 0's moments are not needed afterwards), so that every pad_rfft or column
+// pass CTA reads them instead of reducing all rows again.
 __global__ void norm_constants_kernel(double* __restrict__ rowstats, int n_c, int h, int norm_h, int norm_w) {
   const int c = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   if (c >= n_c) return;
@@ -17,10 +17,12 @@ __global__ void norm_constants_kernel(double* __restrict__ rowstats, int n_c, in
   float e = 0.f, s = 0.f;
   projection_norm_constants(rs, h, norm_h, norm_w, &e, &s);
   __syncwarp();
-  if ((threadIdx.x & 31) == 0) {
-    rs[0] = (double)e;
-    rs[1] = (double)s;
-  }
+  if ((threadIdx.x & 31) == 0) *reinterpret_cast<float2*>(rs) = make_float2(e, s);
+}
+
+int launch_norm_constants(double* rowstats, int n_c, int h, int norm_h, int norm_w, cudaStream_t s) {
+  norm_constants_kernel<<<(n_c + 7) / 8, 256, 0, s>>>(rowstats, n_c, h, norm_h, norm_w);
+  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
 
@@ -55,8 +57,8 @@ static int pad_rfft_t(const float* proj, const double* rowstats, int h, int norm
   // otherwise reduce all h rows in FP64); a few CTAs do it themselves
   const int ready = ctas >= 16;
   if (ready) {
-    norm_constants_kernel<<<(n_c + 7) / 8, 256, 0, s>>>(const_cast<double*>(rowstats), n_c, h, norm_h, norm_w);
-    if (cudaGetLastError() != cudaSuccess) return LGB_ERR_CUDA;
+    const int st = launch_norm_constants(const_cast<double*>(rowstats), n_c, h, norm_h, norm_w, s);
+    if (st) return st;
   }
   dim3 grid(ctas, n_c);
   // shared twiddle tables where a CTA transforms >= 4 rows

@@ -506,6 +506,8 @@ int lgb_refine_search(const lgb_refine_problem* p, const lgb_ctf_params* ctf, co
   if (cudaGetLastError() != cudaSuccess) return LGB_ERR_CUDA;
   const float scale = 1.0f / ((float)H * (float)W);
   const bool prof = profiling_on();
+  // square crops of 288 with a 256 template: projection row pass and padded rfft fused
+  const bool fused_rfft = supported_proj_row_rfft(d, W) && H == 288;
   int st;
   for (int o0 = 0; o0 < p->n_offsets; o0 += p->offset_batch) {
     const int nb = (p->n_offsets - o0) < p->offset_batch ? (p->n_offsets - o0) : p->offset_batch;
@@ -521,17 +523,37 @@ int lgb_refine_search(const lgb_refine_problem* p, const lgb_ctf_params* ctf, co
       StageScope sc(LGB_STAGE_PROJ_COL, s, prof);
       if ((st = launch_proj_col(d, slices, filt, nb, L.n_cd, n_c, T, s))) return st;
     }
-    {
-      StageScope sc(LGB_STAGE_PROJ_ROW, s, prof);
-      if ((st = launch_proj_row(d, T, n_c, proj, rowstats, s))) return st;
-    }
-    {
-      StageScope sc(LGB_STAGE_PAD_RFFT, s, prof);
-      if ((st = launch_pad_rfft(W, proj, rowstats, d, H, W, L.wcp, n_c, A, s))) return st;
-    }
-    {
-      StageScope sc(LGB_STAGE_COLPASS, s, prof);
-      if ((st = launch_colpass(H, A, ip, d, L.wcp, n_c, n_cpp, L.crop_h, 0, Y, s))) return st;
+    if (fused_rfft) {
+      // the projection stays on chip: row c2r + padded rfft of the raw row, and
+      // the normalisation s (A - e U) applied by the column pass
+      {
+        StageScope sc(LGB_STAGE_PROJ_ROW, s, prof);
+        if ((st = launch_proj_row_rfft(d, W, T, n_c, rowstats, L.wcp, A, s))) return st;
+      }
+      {
+        StageScope sc(LGB_STAGE_PAD_RFFT, s, prof);
+        if ((st = launch_norm_constants(rowstats, n_c, d, H, W, s))) return st;
+      }
+      {
+        StageScope sc(LGB_STAGE_COLPASS, s, prof);
+        // (e, s) of correlogram c: float2 at rowstats[c][0][0], d * 3 doubles apart
+        if ((st = launch_colpass(H, A, ip, d, L.wcp, n_c, n_cpp, L.crop_h, 0, Y, s,
+                                 reinterpret_cast<const float2*>(rowstats), d * 3, W)))
+          return st;
+      }
+    } else {
+      {
+        StageScope sc(LGB_STAGE_PROJ_ROW, s, prof);
+        if ((st = launch_proj_row(d, T, n_c, proj, rowstats, s))) return st;
+      }
+      {
+        StageScope sc(LGB_STAGE_PAD_RFFT, s, prof);
+        if ((st = launch_pad_rfft(W, proj, rowstats, d, H, W, L.wcp, n_c, A, s))) return st;
+      }
+      {
+        StageScope sc(LGB_STAGE_COLPASS, s, prof);
+        if ((st = launch_colpass(H, A, ip, d, L.wcp, n_c, n_cpp, L.crop_h, 0, Y, s))) return st;
+      }
     }
     {
       StageScope sc(LGB_STAGE_ROWPASS, s, prof);
