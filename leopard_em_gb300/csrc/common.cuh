@@ -18,6 +18,18 @@ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
 }
 __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+
+// float -> double with integer operations (exponent re-bias, mantissa shift):
+// exact for normal floats, which leaves the FP64 pipe (about one operation per
+// SM per clock on this GPU, conversions included) to the additions.  Zero,
+// subnormal, inf and nan go through the converter.
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned ex = (u >> 23) & 0xffu;
+  if (ex == 0u || ex == 0xffu) return (double)f;
+  const unsigned hi = (u & 0x80000000u) | ((ex + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+  return __hiloint2double((int)hi, (int)(u << 29));
+}
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 // multiply by DIR*i  (DIR = +1: i, DIR = -1: -i)
 template <int DIR>

@@ -553,10 +553,10 @@ __global__ void __launch_bounds__(NT, 2)
         const int cc = barg[o + 1];
         bi.y = (cc / nb) * n_orient + o0 + (cc - (cc / nb) * nb);
       }
-      sa.x += (double)bs[o];
-      sa.y += (double)bs[o + 1];
-      sq.x += (double)bss[o];
-      sq.y += (double)bss[o + 1];
+      sa.x += f2d_bits(bs[o]);
+      sa.y += f2d_bits(bs[o + 1]);
+      sq.x += f2d_bits(bss[o]);
+      sq.y += f2d_bits(bss[o + 1]);
       *reinterpret_cast<float2*>(mip + idx) = mm;
       *reinterpret_cast<int2*>(best + idx) = bi;
       *reinterpret_cast<double2*>(s1 + idx) = sa;

@@ -693,10 +693,10 @@ __global__ void __launch_bounds__(NT, 2)
       const int cc = barg[2 * r + 1];
       bi.y = (cc / nb) * n_orient + o0 + (cc - (cc / nb) * nb);
     }
-    a.x += (double)bs[2 * r];
-    a.y += (double)bs[2 * r + 1];
-    q.x += (double)bss[2 * r];
-    q.y += (double)bss[2 * r + 1];
+    a.x += f2d_bits(bs[2 * r]);
+    a.y += f2d_bits(bs[2 * r + 1]);
+    q.x += f2d_bits(bss[2 * r]);
+    q.y += f2d_bits(bss[2 * r + 1]);
     *reinterpret_cast<float2*>(mip + idx) = m;
     *reinterpret_cast<int2*>(best + idx) = bi;
     *reinterpret_cast<double2*>(s1 + idx) = a;
