@@ -352,9 +352,13 @@ __global__ void __launch_bounds__(ROWS * 16)
   constexpr int C2 = 8;    // c2r: M = 16 x 8
   constexpr int R2 = 9;    // rfft: WH = 16 x 9
   constexpr int ZR = IdxPad16::pad(WH) + 2;
-  __shared__ float2 xin[ROWS][WC + 1];
+  static_assert(ZR >= WC + 1, "staged row fits the rfft buffer");
+  // xin (the staged row of T, read only by c2r pass 1) and zr (the rfft input,
+  // written from c2r pass 2 on, then Z) share one buffer per row
+  __shared__ float2 xz[ROWS][ZR];
   __shared__ float2 zb[ROWS][R2 * S1 + 1];  // c2r transpose (8 x 17), then rfft transpose (9 x 17)
-  __shared__ float2 zr[ROWS][ZR];           // rfft input z[m'] (zero for m' >= 128), then Z
+  float2(*xin)[ZR] = xz;
+  float2(*zr)[ZR] = xz;
   __shared__ float2 pre[M];                 // exp(+i pi k / M)
   __shared__ float2 rootc[15 * (C2 - 1) + 1];  // exp(+2 pi i m / M)
   __shared__ float2 rootr[15 * (R2 - 1) + 1];  // exp(-2 pi i m / WH)
@@ -363,16 +367,6 @@ __global__ void __launch_bounds__(ROWS * 16)
     float sn, cs;
     sincospif((float)k / (float)M, &sn, &cs);
     pre[k] = make_float2(cs, sn);
-  }
-  for (int m = threadIdx.x; m < 15 * (C2 - 1) + 1; m += blockDim.x) {
-    float sn, cs;
-    sincospif(2.0f * (float)m / (float)M, &sn, &cs);
-    rootc[m] = make_float2(cs, sn);
-  }
-  for (int m = threadIdx.x; m < 15 * (R2 - 1) + 1; m += blockDim.x) {
-    float sn, cs;
-    sincospif(2.0f * (float)m / (float)WH, &sn, &cs);
-    rootr[m] = make_float2(cs, -sn);
   }
   for (int k = threadIdx.x; k <= WH; k += blockDim.x) {
     float sn, cs;
@@ -385,6 +379,17 @@ __global__ void __launch_bounds__(ROWS * 16)
   const float2* src = T + ((size_t)c * HT + row0) * WC;
   for (int e = threadIdx.x; e < ROWS * WC; e += blockDim.x) xin[e / WC][e % WC] = src[e];
   __syncthreads();
+  // the radix roots are the pre- and post-twiddles at even angles:
+  // exp(+2 pi i m / M) = +-pre[2m mod M], exp(-2 pi i m / WH) = +-post[2m mod WH]
+  // (read from the next pass on, after a barrier)
+  for (int m = threadIdx.x; m < 15 * (C2 - 1) + 1; m += blockDim.x) {
+    const float2 v = pre[(2 * m) & (M - 1)];
+    rootc[m] = 2 * m < M ? v : make_float2(-v.x, -v.y);
+  }
+  for (int m = threadIdx.x; m < 15 * (R2 - 1) + 1; m += blockDim.x) {
+    const float2 v = post[2 * m <= WH ? 2 * m : 2 * m - WH];
+    rootr[m] = 2 * m <= WH ? v : make_float2(-v.x, -v.y);
+  }
   // ---- c2r pass 1 (radix 16) on the pre-twiddled z[k], k = t + 8q
   if (t < C2) {
     float2 v[16];

@@ -125,7 +125,8 @@ bool supported_proj_row_rfft(int h, int W) { return h == 256 && W == 288; }
 
 int launch_proj_row_rfft(int h, int W, const void* T, int n_c, double* rowstats, int Wcp, void* A, cudaStream_t s) {
   if (!supported_proj_row_rfft(h, W) || Wcp < W / 2 + 1) return LGB_ERR_UNSUPPORTED_SIZE;
-  proj_row_rfft_kernel<kProjRows><<<dim3(256 / kProjRows, n_c), kProjRows * 16, 0, s>>>(
+  // 16 rows per CTA: the twiddle tables are built once per 16 rows
+  proj_row_rfft_kernel<16><<<dim3(256 / 16, n_c), 16 * 16, 0, s>>>(
       static_cast<const float2*>(T), rowstats, Wcp, static_cast<float2*>(A));
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
