@@ -15,6 +15,10 @@
 //   rowpass_kernel    per row: c2r of length W (1/(H W)) and the fused
 //                     statistics update (utils.py:191-255): max over the
 //                     batch, strict '>' MIP update, global index, FP64 sums
+// Two-register-pass forms for the refinement crops (288^2, d = 256):
+// proj_col_pair_kernel (256 = 16 x 16) and proj_row_rfft_kernel (row c2r
+// 16 x 8 and the padded rfft 16 x 9 in one kernel; the normalisation moves to
+// the column pass, colpass_pair_kernel in match_fused.cuh).
 #pragma once
 
 #include "fft.cuh"

@@ -4,9 +4,11 @@
 // x C pixel-size offsets.  Per offset batch (B offsets, n_cpp = C*D*B
 // correlograms per particle, c = (cs*D + df)*B + b):
 //   refine_rotations_kernel  R = R(offset) @ R(particle)            (FP64)
-//   slice / proj_col / proj_row / pad_rfft / colpass                (shared with the search)
+//   slice / proj_col / proj_row / pad_rfft / colpass                (shared with the search;
+//                            288^2 crops with d = 256: proj_row + pad_rfft fused, the
+//                            normalisation applied by the column pass)
 //   refine_rowpass_kernel    rows y < crop_h only: c2r, valid crop, z = (cc - mean)/std,
-//                            packed (z, pixel-major flat index) arg-max and max cc per particle
+//   (_pair for W = 288)      packed (z, pixel-major flat index) arg-max and max cc per particle
 //   refine_commit_kernel     strict '>' against the particle's best so far
 // The filters (per-particle projective filter x CTF stack with B envelope) are
 // built once per call by refine_filters_kernel.
