@@ -386,6 +386,10 @@ static bool valid_refine(const lgb_refine_problem* p) {
          p->n_particles > 0;
 }
 
+// 288^2 crops with a 256 template: the projection row pass and the padded
+// rfft run fused (no projection buffer) and the column pass normalises
+static bool refine_fused_rfft(int d, int W, int H) { return supported_proj_row_rfft(d, W) && H == 288; }
+
 static RefineLayout refine_layout(const lgb_refine_problem* p) {
   RefineLayout L{};
   const size_t H = p->image_h, W = p->image_w, d = p->template_size, P = p->n_particles;
@@ -408,7 +412,7 @@ static RefineLayout refine_layout(const lgb_refine_problem* p) {
   L.t = off;
   off += al256(nc * d * L.wc_t * sizeof(float2));
   L.proj = off;
-  off += al256(nc * d * d * sizeof(float));
+  off += refine_fused_rfft((int)d, (int)W, (int)H) ? 0 : al256(nc * d * d * sizeof(float));
   L.rowstats = off;
   off += al256(nc * d * 3 * sizeof(double));
   L.a = off;
@@ -508,8 +512,7 @@ int lgb_refine_search(const lgb_refine_problem* p, const lgb_ctf_params* ctf, co
   if (cudaGetLastError() != cudaSuccess) return LGB_ERR_CUDA;
   const float scale = 1.0f / ((float)H * (float)W);
   const bool prof = profiling_on();
-  // square crops of 288 with a 256 template: projection row pass and padded rfft fused
-  const bool fused_rfft = supported_proj_row_rfft(d, W) && H == 288;
+  const bool fused_rfft = refine_fused_rfft(d, W, H);
   int st;
   for (int o0 = 0; o0 < p->n_offsets; o0 += p->offset_batch) {
     const int nb = (p->n_offsets - o0) < p->offset_batch ? (p->n_offsets - o0) : p->offset_batch;
