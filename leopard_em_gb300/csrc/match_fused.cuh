@@ -414,7 +414,7 @@ struct RowFused {
 };
 
 template <int WH, int NT, class RL>
-__global__ void __launch_bounds__(NT, 2)
+__global__ void __launch_bounds__(NT, 3)
     rowpass_fused_kernel(const float2* __restrict__ Y, int y_rows, int Wcp, int n_c, int nb, int n_orient, int o0,
                          const int* __restrict__ o0_dev, float scale, float* __restrict__ mip,
                          int* __restrict__ best, double* __restrict__ s1, double* __restrict__ s2) {
@@ -449,14 +449,15 @@ __global__ void __launch_bounds__(NT, 2)
   const float2* tab_last = tab + TableSize<1, typename DropLast<RL>::type>::value;
 
   float bmax[2 * OUT], bs[2 * OUT], bss[2 * OUT];
-  int barg[2 * OUT];
+  unsigned barg[OUT];  // batch index of each pixel pair's maxima: low / high 16 bits
 #pragma unroll
   for (int i = 0; i < 2 * OUT; ++i) {
     bmax[i] = -INFINITY;
-    barg[i] = 0;
     bs[i] = 0.f;
     bss[i] = 0.f;
   }
+#pragma unroll
+  for (int i = 0; i < OUT; ++i) barg[i] = 0u;
 
 #pragma unroll 1
   for (int c = 0; c < n_c; ++c) {
@@ -519,8 +520,9 @@ __global__ void __launch_bounds__(NT, 2)
       for (int q = 0; q < RLAST; ++q) {
         const int o = 2 * (p * RLAST + q);
         const float a = v[q].x * scale, b = v[q].y * scale;
-        if (a > bmax[o]) { bmax[o] = a; barg[o] = c; }
-        if (b > bmax[o + 1]) { bmax[o + 1] = b; barg[o + 1] = c; }
+        const int k = p * RLAST + q;
+        if (a > bmax[o]) { bmax[o] = a; barg[k] = (barg[k] & 0xffff0000u) | (unsigned)c; }
+        if (b > bmax[o + 1]) { bmax[o + 1] = b; barg[k] = (barg[k] & 0xffffu) | ((unsigned)c << 16); }
         bs[o] += a;
         bss[o] = fmaf(a, a, bss[o]);
         bs[o + 1] += b;
@@ -545,12 +547,12 @@ __global__ void __launch_bounds__(NT, 2)
       double2 sq = *reinterpret_cast<double2*>(s2 + idx);
       if (bmax[o] > mm.x) {
         mm.x = bmax[o];
-        const int cc = barg[o];
+        const int cc = (int)(barg[p * RLAST + q] & 0xffffu);
         bi.x = (cc / nb) * n_orient + o0 + (cc - (cc / nb) * nb);
       }
       if (bmax[o + 1] > mm.y) {
         mm.y = bmax[o + 1];
-        const int cc = barg[o + 1];
+        const int cc = (int)(barg[p * RLAST + q] >> 16);
         bi.y = (cc / nb) * n_orient + o0 + (cc - (cc / nb) * nb);
       }
       sa.x += f2d_bits(bs[o]);

@@ -100,9 +100,12 @@ template <int WH, int NT, class RL>
 static int rowpass_fused_t(const void* Y, int H, int y_rows, int Wcp, int n_c, int nb, int n_orient, int o0,
                            const int* o0_dev, float* mip, int* best, double* s1, double* s2, cudaStream_t s) {
   using RF = RowFused<WH, NT, RL>;
+  if (n_c > 0xffff) return LGB_ERR_INVALID_ARGUMENT;  // batch indices are kept in 16 bits
   const size_t smem = RF::smem(Wcp);
   if (cudaFuncSetAttribute(rowpass_fused_kernel<WH, NT, RL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem) != cudaSuccess)
+                           (int)smem) != cudaSuccess ||
+      cudaFuncSetAttribute(rowpass_fused_kernel<WH, NT, RL>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           cudaSharedmemCarveoutMaxShared) != cudaSuccess)
     return LGB_ERR_CUDA;
   const float scale = 1.0f / ((float)H * (float)(2 * WH));
   rowpass_fused_kernel<WH, NT, RL><<<y_rows, NT, smem, s>>>(static_cast<const float2*>(Y), y_rows, Wcp, n_c, nb,
