@@ -68,6 +68,10 @@ def _args():
     ap.add_argument("--refine-plain-only", action="store_true",
                     help="only time the plain refinement grid on --refine-particles particles (profiling)")
     ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--no-torch-reference", action="store_true",
+                    help="skip timing the reference's torch + cuFFT GPU path on this GPU")
+    ap.add_argument("--torch-ref-batches", type=int, default=4)
+    ap.add_argument("--torch-ref-streams", type=int, default=4)
     ap.add_argument("--precision-error-orient", type=int, default=256,
                     help="orientations of the small configuration checked against the FP64 oracle")
     ap.add_argument("--batched-micrographs", type=int, default=12)
@@ -158,8 +162,12 @@ def _fp32_peak(dev):
     """Non-tensor FP32 peak (TFLOP/s) from the library's FMA probe, best of 3."""
     import ctypes
 
-    from leopard_em_gb300._native import check, lib
+    from leopard_em_gb300._native import check
+    from leopard_em_gb300.build import PROBE_LIB_PATH
 
+    probe = ctypes.CDLL(PROBE_LIB_PATH)
+    probe.lgb_fp32_fma_probe.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    probe.lgb_fp32_fma_probe.restype = ctypes.c_int
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     blocks, iters = sms * 8, 20000
     out = torch.zeros(1, device=dev)
@@ -171,7 +179,7 @@ def _fp32_peak(dev):
         a = torch.cuda.Event(enable_timing=True)
         z = torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        check(lib().lgb_fp32_fma_probe(blocks, iters, out.data_ptr(), s), "lgb_fp32_fma_probe")
+        check(probe.lgb_fp32_fma_probe(blocks, iters, out.data_ptr(), s), "lgb_fp32_fma_probe")
         z.record(stream)
         z.synchronize()
         if i:
@@ -197,6 +205,157 @@ def _peaks():
             return json.load(f), "measured"
     except Exception:
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# The reference's own GPU path, torch + cuFFT, timed on this GPU.  Restates the
+# operation sequence of Leopard-EM's default ("streamed") search backend:
+# do_streamed_orientation_cross_correlate (backend/cross_correlation.py:13-154)
+# with round-robin CUDA streams, normalize_template_projection
+# (backend/utils.py:106-188) and do_iteration_statistics_updates
+# (utils.py:191-255), both torch.compile'd as the reference does (utils.py:259-266;
+# eager when compilation fails), inside the orientation loop of
+# _core_match_template_single_gpu (backend/core_match_template.py:492-550).
+# Central slices (torch-fourier-slice) are a trilinear gather in torch ops.
+# ---------------------------------------------------------------------------
+def _ref_normalize(projections, small_shape, large_shape):
+    top, bottom = projections[..., 0, :], projections[..., -1, :]
+    left, right = projections[..., 1:-1, 0], projections[..., 1:-1, -1]
+    edge = torch.concatenate([top, bottom, left, right], dim=-1)
+    projections = projections - edge.mean(dim=-1)[..., None, None]
+    large_sqrt = (large_shape[0] * large_shape[1]) ** 0.5
+    rel = (small_shape[0] * small_shape[1]) / (large_shape[0] * large_shape[1])
+    mean = torch.mean(projections, dim=(-2, -1), keepdim=True) * rel * rel
+    var = torch.sum((projections - mean) ** 2, dim=(-2, -1), keepdim=True)
+    var = var + (large_shape[0] - small_shape[0]) * (large_shape[1] - small_shape[1]) * mean**2
+    return (projections * large_sqrt) / torch.sqrt(var.clamp_min(1e-8))
+
+
+def _ref_stats_update(cc, idx, mip, best, s1, s2, h, w):
+    ccr = cc.reshape(-1, h, w)
+    mv, mi = torch.max(ccr, dim=0)
+    upd = mv > mip
+    mip.copy_(torch.where(upd, mv, mip))
+    best.copy_(torch.where(upd, idx[mi], best))
+    s1 += ccr.sum(dim=0)
+    s2 += (ccr**2).sum(dim=0)
+
+
+def _ref_slices(vol, rot):
+    """Central slices (B, d, d//2+1) of the fftshifted rfft volume, trilinear,
+    Friedel mate for x < 0, zero outside (torch-fourier-slice convention)."""
+    d = vol.shape[0]
+    dev = vol.device
+    fy = torch.fft.fftshift(torch.fft.fftfreq(d, device=dev))
+    fx = torch.fft.rfftfreq(d, device=dev)
+    gy, gx = torch.meshgrid(fy, fx, indexing="ij")
+    zyx = torch.stack([torch.zeros_like(gy), gy, gx], dim=-1)
+    r = torch.einsum("bij,hwj->bhwi", torch.flip(rot, dims=(-2, -1)), zyx)
+    conj = r[..., 2] < 0
+    r = torch.where(conj[..., None], -r, r)
+    c = r * d + torch.tensor([d // 2, d // 2, 0.0], device=dev)
+    hi = torch.tensor(vol.shape, device=dev, dtype=c.dtype) - 1
+    inside = ((c >= 0) & (c <= hi)).all(dim=-1)
+    c = torch.minimum(c.clamp_min(0), hi)
+    i0 = c.floor().long()
+    t = c - i0
+    i1 = torch.minimum(i0 + 1, hi.long())
+    out = torch.zeros(c.shape[:-1], dtype=vol.dtype, device=dev)
+    for dz in (0, 1):
+        for dy in (0, 1):
+            for dx in (0, 1):
+                iz = (i1 if dz else i0)[..., 0]
+                iy = (i1 if dy else i0)[..., 1]
+                ix = (i1 if dx else i0)[..., 2]
+                wgt = ((t[..., 0] if dz else 1 - t[..., 0]) * (t[..., 1] if dy else 1 - t[..., 1])
+                       * (t[..., 2] if dx else 1 - t[..., 2]))
+                out = out + vol[iz, iy, ix] * wgt
+    out = torch.where(inside, out, torch.zeros_like(out))
+    return torch.where(conj, out.conj(), out)
+
+
+def _euler_zyz(e):
+    a, b, c = (torch.deg2rad(e[:, i].double()) for i in range(3))
+
+    def rz(t):
+        o, z = torch.ones_like(t), torch.zeros_like(t)
+        return torch.stack([torch.cos(t), -torch.sin(t), z, torch.sin(t), torch.cos(t), z, z, z, o], -1).view(-1, 3, 3)
+
+    def ry(t):
+        o, z = torch.ones_like(t), torch.zeros_like(t)
+        return torch.stack([torch.cos(t), z, torch.sin(t), z, o, z, -torch.sin(t), z, torch.cos(t)], -1).view(-1, 3, 3)
+
+    return (rz(a) @ ry(b) @ rz(c)).float()
+
+
+def torch_cufft_reference(kw, dev, batch, n_batches, n_streams):
+    """Orientations/s of the reference's torch + cuFFT GPU path on this GPU
+    (same inputs, batch ``batch``, ``n_streams`` CUDA streams), device-timed
+    over ``n_batches`` batches after one warm-up batch."""
+    image_dft = kw["image_dft"].to(dev)
+    template_dft = kw["template_dft"].to(dev)
+    pf = (kw["ctf_filters"] * kw["whitening_filter_template"][None, None]).to(dev)
+    eul = kw["euler_angles"].to(dev)
+    n_cs, n_df = pf.shape[0], pf.shape[1]
+    H, W = image_dft.shape[0], 2 * image_dft.shape[1] - 2
+    small = (template_dft.shape[1], 2 * template_dft.shape[2] - 2)
+    compiled = "inductor (default mode)"
+    try:
+        norm = torch.compile(_ref_normalize)
+        upd = torch.compile(_ref_stats_update)
+        norm(torch.randn(2, *small, device=dev), small, (H, W))
+    except Exception as e:  # the reference falls back to eager the same way (utils.py:92-100)
+        norm, upd, compiled = _ref_normalize, _ref_stats_update, f"eager ({type(e).__name__})"
+    streams = [torch.cuda.Stream(dev) for _ in range(n_streams)]
+    mip = torch.full((H, W), -float("inf"), device=dev)
+    best = torch.full((H, W), -1, dtype=torch.int32, device=dev)
+    s1 = torch.zeros((H, W), device=dev)
+    s2 = torch.zeros((H, W), device=dev)
+    n_o = eul.shape[0]
+    incr = torch.tensor([df * n_o + cs * n_df * n_o for cs in range(n_cs) for df in range(n_df)], device=dev)
+
+    def one_batch(o0):
+        rot = _euler_zyz(eul[o0:o0 + batch])
+        fs = _ref_slices(template_dft, rot)
+        fs = torch.fft.ifftshift(fs, dim=(-2,))
+        fs[..., 0, 0] = 0
+        fs *= -1
+        cc = torch.empty((n_cs, n_df, rot.shape[0], H, W), device=dev)
+        default = torch.cuda.current_stream(dev)
+        for st in streams:
+            st.wait_stream(default)
+        for i in range(rot.shape[0]):
+            for j in range(n_df):
+                for k in range(n_cs):
+                    st = streams[(i * n_df * n_cs + j * n_cs + k) % n_streams]  # round robin
+                    with torch.cuda.stream(st):
+                        proj = torch.fft.irfft2(fs[i] * pf[k, j])
+                        proj = torch.fft.ifftshift(proj, dim=(-2, -1))
+                        proj = norm(proj, small, (H, W))
+                        tmp = torch.fft.rfft(proj, n=W, dim=-1)
+                        pd = torch.fft.fft(tmp, n=H, dim=-2)
+                        pd[0, 0] = 0
+                        torch.fft.irfft2(image_dft * pd.conj(), s=(H, W), out=cc[k, j, i])
+        for st in streams:
+            default.wait_stream(st)
+        fs.record_stream(default)
+        idx = (torch.arange(o0, o0 + rot.shape[0], device=dev) + incr[:, None]).flatten().to(torch.int32)
+        upd(cc, idx, mip, best, s1, s2, H, W)
+
+    one_batch(0)
+    torch.cuda.synchronize(dev)
+    stream = torch.cuda.current_stream(dev)
+    a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for b in range(n_batches):
+        one_batch(((b + 1) * batch) % max(1, n_o - batch))
+    z.record(stream)
+    torch.cuda.synchronize(dev)
+    sec = a.elapsed_time(z) / 1e3
+    n = n_batches * batch
+    return {"value": n / sec, "unit": UNIT, "cross_correlations_per_s": n * n_cs * n_df / sec,
+            "orientations": n, "orientation_batch": batch, "cuda_streams": n_streams, "compiled": compiled,
+            "path": "torch.fft (cuFFT) restatement of the reference's streamed GPU backend, same inputs"}
 
 
 def precision_bench(args, dev):
@@ -643,6 +802,13 @@ def main():
                "sample": f"{n} orientations x {n_cd} defocus of the {cfg.name} workload, CPU oracle "
                          "(torch.fft/pocketfft restatement of the reference's CPU path)"}
 
+    torch_ref = None
+    if rank == 0 and world == 1 and not args.no_torch_reference:
+        torch_ref = torch_cufft_reference(kw, dev, B, args.torch_ref_batches, args.torch_ref_streams)
+        torch_ref["value_over_torch_cufft"] = value / torch_ref["value"]
+        if e2e_val:
+            torch_ref["e2e_over_torch_cufft"] = e2e_val / torch_ref["value"]
+
     refine = None
     if rank == 0 and world == 1 and not args.no_refine:
         refine = refine_bench(args, dev, with_cpu=not args.no_cpu_baseline)
@@ -668,7 +834,8 @@ def main():
                     "orientations_per_call": e2e_chunk, "two_run_model": two_run,
                     "timing": "wall clock per core_match_template call on pinned host tensors: upload, search, "
                               "finalize, all maps back to the host"},
-            "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": gpu_launches,
+            "roofline": roofline, "cpu_baseline": cpu, "gpu_torch_baseline": torch_ref,
+            "gpu_launches": gpu_launches,
             "clocks": clocks.summary(),
             "refine": refine,
             "batched": batched,

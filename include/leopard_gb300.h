@@ -86,12 +86,6 @@ const char* lgb_status_string(int status);
 /* Library version, major*10000 + minor*100 + patch. */
 int lgb_version(void);
 
-/* FP32 FMA throughput probe (measurement only): `blocks` CTAs of 256 threads,
- * each thread running 8 independent chains of iters*16 FMAs (2 FLOPs each);
- * time it with events to get the non-tensor FP32 peak.  `out` (device float)
- * is only written if a chain sums to a sentinel (never in practice). */
-int lgb_fp32_fma_probe(int blocks, int iters, float* out, void* stream);
-
 /* Stage profiler (no reference counterpart; measurement only).  Between
  * lgb_profile_begin and lgb_profile_end every stage launch made by
  * lgb_match_search on any stream is bracketed by CUDA events on that stream.

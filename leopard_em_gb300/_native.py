@@ -79,7 +79,6 @@ _SIGNATURES = {
     "lgb_status_string": ([_I], ctypes.c_char_p),
     "lgb_version": ([], _I),
     "lgb_profile_begin": ([], _I),
-    "lgb_fp32_fma_probe": ([_I, _I, _P, _P], _I),
     "lgb_profile_end": ([ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_LL), _I], _I),
     "lgb_match_supported": ([_PROB], _I),
     "lgb_match_workspace_size": ([_PROB, ctypes.POINTER(_SZ)], _I),

@@ -103,15 +103,25 @@ struct SearchArgs {
   double* s2;
 };
 
-static int search_args(const lgb_match_problem* p, const void* template_dft, const float* pf, const float* euler,
-                       int begin, int end, float* mip, int* best, double* s1, double* s2, void* workspace,
-                       size_t workspace_bytes, SearchArgs* a) {
-  if (!valid_problem(p) || !template_dft || !pf || !euler || !mip || !best || !s1 || !s2 || !workspace)
+int check_search_args(const lgb_match_problem* p, const void* template_dft, const float* pf, const float* euler,
+                      int begin, int end, const float* mip, const int* best, const double* s1, const double* s2) {
+  if (!valid_problem(p) || !template_dft || !pf || !euler || !mip || !best || !s1 || !s2)
     return LGB_ERR_INVALID_ARGUMENT;
   if (begin < 0 || end > p->n_orientations || begin > end) return LGB_ERR_INVALID_ARGUMENT;
   if (!lgb_match_supported(p)) return LGB_ERR_UNSUPPORTED_SIZE;
   const long long total_idx = (long long)p->n_orientations * p->n_defocus * p->n_pixel_sizes;
   if (total_idx > 2147483647LL) return LGB_ERR_INVALID_ARGUMENT;  // int32 global index, as the reference
+  // the row pass keeps each pixel's batch argmax in 16 bits
+  if ((long long)p->n_pixel_sizes * p->n_defocus * p->orientation_batch > 0xffff) return LGB_ERR_INVALID_ARGUMENT;
+  return LGB_OK;
+}
+
+static int search_args(const lgb_match_problem* p, const void* template_dft, const float* pf, const float* euler,
+                       int begin, int end, float* mip, int* best, double* s1, double* s2, void* workspace,
+                       size_t workspace_bytes, SearchArgs* a) {
+  const int st = check_search_args(p, template_dft, pf, euler, begin, end, mip, best, s1, s2);
+  if (st != LGB_OK) return st;
+  if (!workspace) return LGB_ERR_INVALID_ARGUMENT;
   a->p = p;
   a->L = layout_of(p);
   if (workspace_bytes < a->L.total) return LGB_ERR_WORKSPACE_TOO_SMALL;

@@ -1,7 +1,9 @@
 // FP32 FMA throughput probe: the non-tensor FP32 peak of this GPU (the
 // denominator of the FFT kernels' compute roofline), measured with
-// independent FMA chains in registers.
-#include "common.cuh"
+// independent FMA chains in registers.  Measurement only: it is linked into
+// its own library (_build/libleopard_gb300_probe.so), which the benchmark
+// loads; the product library does not carry it.
+#include "../common.cuh"
 
 namespace lgb {
 

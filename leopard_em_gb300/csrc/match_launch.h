@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 
+#include "../../include/leopard_gb300.h"
+
 namespace lgb {
 
 // Each returns an lgb_status; LGB_ERR_UNSUPPORTED_SIZE when the FFT length is
@@ -47,6 +49,11 @@ int launch_colpass(int H, const void* A, const void* Ip, int h, int Wcp, int n_c
 // index base o0 + *o0_dev (o0_dev may be null).
 int launch_rowpass(int W, const void* Y, int H, int y_rows, int Wcp, int n_c, int nb, int n_orient, int o0,
                    const int* o0_dev, float* mip, int* best, double* s1, double* s2, cudaStream_t s);
+
+// Every argument check of lgb_match_search except the workspace; LGB_OK or
+// the status lgb_match_search would return.  Runs no GPU work.
+int check_search_args(const lgb_match_problem* p, const void* template_dft, const float* pf, const float* euler,
+                      int begin, int end, const float* mip, const int* best, const double* s1, const double* s2);
 
 bool supported_template(int h);
 bool supported_row(int W);

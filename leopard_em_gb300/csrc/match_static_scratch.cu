@@ -17,7 +17,12 @@
 //     library holds these 32 MiB until the process exits;
 //   * the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (with that device current) and caches it; make that
-//     first call before any stream capture on the device;
+//     first call before any stream capture on the device.  The cached address
+//     belongs to the device's primary context: the library must not be used
+//     again on a device after cudaDeviceReset (which destroys that context and
+//     the array with it);
+//   * every argument is checked before any GPU work: a rejected call leaves
+//     the array untouched;
 //   * all calls share the one array, which keeps the last call's contents.
 //     Every byte the kernels read is rewritten earlier in the same call (the
 //     image spectrum is repacked, zero padding included, at the start of each
@@ -69,6 +74,10 @@ int lgb_match_search_static_scratch(const lgb_match_problem* problem, const void
   if (st != LGB_OK) return st;
   if (need > lgb::kStaticScratchBytes) return LGB_ERR_WORKSPACE_TOO_SMALL;
   if (!image_dft) return LGB_ERR_INVALID_ARGUMENT;
+  // all of lgb_match_search's checks before the image repack touches the array
+  if ((st = lgb::check_search_args(problem, template_dft, projective_filters, euler_angles, orientation_begin,
+                                   orientation_end, mip, best_index, corr_sum, corr_sq_sum)) != LGB_OK)
+    return st;
   void* scratch = nullptr;
   if ((st = lgb::static_scratch_address(&scratch)) != LGB_OK) return st;
   if ((st = lgb_match_prepare_image(problem, image_dft, scratch, lgb::kStaticScratchBytes, stream)) != LGB_OK)

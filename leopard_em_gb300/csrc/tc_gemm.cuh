@@ -28,7 +28,10 @@
 // TMEM columns; all four warps then read their 32 TMEM lanes (rows) back
 // with tcgen05.ld and hand them to the epilogue.  Every wait is bounded: on
 // timeout the CTA records LGB_ERR_DEVICE_TIMEOUT in *err, waits (bounded) for
-// its in-flight MMAs, frees its TMEM and returns.
+// its in-flight bulk copies and MMAs, frees its TMEM and returns.  If one of
+// those last waits also runs out, asynchronous work of the CTA may still be
+// pending when it exits: after LGB_ERR_DEVICE_TIMEOUT the caller treats the
+// CUDA context as unusable (no further launches on it).
 #pragma once
 
 #include <stdint.h>
@@ -252,14 +255,20 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     };
     const uint32_t idesc = mma_idesc(kTcM, BN, F16);
     bool ok = true;
+    int issued = 0, landed = 0;  // chunks whose copies were issued / have been waited for
     load(0);
-    if (KC > 1) load(1);
+    ++issued;
+    if (KC > 1) {
+      load(1);
+      ++issued;
+    }
     for (int kc = 0; kc < KC && ok; ++kc) {
       const int s = kc & 1;
       if (!mbar_wait(&full[s], (kc >> 1) & 1)) {
         ok = false;
         break;
       }
+      ++landed;
       tc_fence_after();
       const uint32_t sa = smem_u32(base + s * S::STAGE);
       const uint32_t sb = sa + 2 * S::A_BYTES;
@@ -283,11 +292,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           break;
         }
         load(kc + 1);
+        ++issued;
       }
     }
     if (!ok) {
       s_fail = 1;
       atomicExch(g.err, LGB_ERR_DEVICE_TIMEOUT);
+      // copies still in flight target this CTA's shared memory: wait (bounded)
+      // for each before the CTA may exit
+      for (int j = landed; j < issued; ++j) mbar_wait(&full[j & 1], (j >> 1) & 1);
     }
     mma_commit(done);  // tracks every MMA this thread issued
   }

@@ -75,8 +75,10 @@ def gather_search_maps(maps: dict, dst: int = 0, group=None) -> dict | None:
     """Gather every rank's maps to ``dst`` and reduce them there.
 
     Collective over ``group``: every rank must call it with maps of the same
-    shapes and dtypes.  Returns the reduced maps on ``dst`` and ``None`` on the
-    other ranks.
+    shapes and dtypes.  ``dst`` is a rank *within* ``group`` (for the default
+    group, the global rank); the maps are reduced in group-rank order, so ties
+    go to the lowest group rank.  Returns the reduced maps on ``dst`` and
+    ``None`` on the other ranks.
     """
     import torch.distributed as dist
 
@@ -84,11 +86,15 @@ def gather_search_maps(maps: dict, dst: int = 0, group=None) -> dict | None:
         raise RuntimeError("gather_search_maps needs an initialised torch.distributed process group")
     rank = dist.get_rank(group)
     world = dist.get_world_size(group)
+    if not 0 <= dst < world:
+        raise ValueError(f"dst={dst} is not a rank of the group (size {world})")
+    # torch.distributed.gather takes the destination as a global rank
+    dst_global = dist.get_global_rank(group, dst) if group is not None else dst
     gathered: dict[str, list[torch.Tensor] | None] = {}
     for k in MAP_KEYS:
         t = maps[k].contiguous()
         bufs = [torch.empty_like(t) for _ in range(world)] if rank == dst else None
-        dist.gather(t, gather_list=bufs, dst=dst, group=group)
+        dist.gather(t, gather_list=bufs, dst=dst_global, group=group)
         gathered[k] = bufs
     if rank != dst:
         return None

@@ -152,6 +152,50 @@ def test_gloo_two_ranks_gather_reduce(case, batch):
                                atol=1e-12)
 
 
+def _subgroup_rank_main(rank, world, port, case, batch, out_path):
+    """Ranks 1 and 2 of a world of 3 form a subgroup and gather to its rank 0
+    (global rank 1); global rank 0 takes no part."""
+    import torch.distributed as dist
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        group = dist.new_group([1, 2])
+        if rank in (1, 2):
+            inp = _inputs(case)
+            n = inp["euler_angles"].shape[0]
+            g = dist.get_rank(group)
+            begin, end = sharding.orientation_shards(n, 2, batch)[g]
+            maps = _oracle_maps(inp, begin, end, batch)
+            red = sharding.gather_search_maps(maps, dst=0, group=group)
+            if g == 0:
+                assert rank == 1
+                torch.save(red, out_path)
+            else:
+                assert red is None
+        dist.barrier()
+    finally:
+        dist.destroy_process_group()
+
+
+def test_gloo_subgroup_gather_uses_group_rank():
+    """``dst`` is a rank within the group: with the group {1, 2} the maps are
+    reduced on global rank 1, and equal one search over all orientations."""
+    case, batch = "a", 4
+    inp = _inputs(case)
+    n = inp["euler_angles"].shape[0]
+    full = _oracle_maps(inp, 0, n, batch)
+    with tempfile.TemporaryDirectory() as d:
+        out_path = os.path.join(d, "reduced.pt")
+        mp.start_processes(_subgroup_rank_main, args=(3, _free_port(), case, batch, out_path), nprocs=3,
+                           join=True, start_method="spawn")
+        red = torch.load(out_path)
+    torch.testing.assert_close(red["mip"], full["mip"], rtol=0, atol=0)
+    assert (red["best_global_index"] == full["best_global_index"]).all()
+    torch.testing.assert_close(red["correlation_sum"], full["correlation_sum"], rtol=1e-12, atol=1e-12)
+
+
 @pytest.mark.gpu
 def test_device_shards_reduce_to_the_full_search():
     """Two orientation shards searched on the device, reduced in rank order and
