@@ -131,24 +131,76 @@ def ctf_filter_stack(
     return torch.stack(stack)
 
 
-def whitening_filter(image_rfft: torch.Tensor, output_shape: tuple[int, int], num_bins: int | None = None):
-    """1/sqrt(radially averaged power) of ``image_rfft`` sampled on ``output_shape``
-    (an rfft grid of real shape output_shape), normalised to max 1."""
+def whitening_filter(image_rfft: torch.Tensor, output_shape: tuple[int, int], num_bins: int | None = None,
+                     max_freq: float | None = 0.5, do_power_spectrum: bool = True):
+    """Whitening filter of ``image_rfft`` sampled on the rfft grid of real shape
+    ``output_shape``, normalised to max 1 (the published construction of
+    torch-fourier-filter's whitening_filter, called at
+    config/correlation_filters.py:97-108): the radially averaged power
+    (|F|^2, or |F| when ``do_power_spectrum`` is False) in ``num_bins`` bins
+    over [0, max_freq] cycles/pixel, inverted (square root for power), and
+    sampled at each output frequency by its nearest bin; frequencies beyond
+    ``max_freq`` take the last bin's value."""
     H = image_rfft.shape[-2]
     W = 2 * (image_rfft.shape[-1] - 1)
     dev = image_rfft.device
+    fmax = 0.5 if max_freq is None else float(max_freq)
+    if fmax <= 0:
+        raise ValueError("max_freq must be > 0")
     ky, kx = rfft_freq_grid((H, W), device=dev)
     r = torch.sqrt(kx**2 + ky**2)
     nb = num_bins or int(max(H, W) // 2 + 1)
-    idx = torch.clamp((r / 0.5 * (nb - 1)).round().long(), 0, nb - 1)
-    power = torch.zeros(nb, dtype=torch.float64, device=dev).index_add_(
-        0, idx.flatten(), (image_rfft.abs() ** 2).flatten().double())
+    idx = torch.clamp((r / fmax * (nb - 1)).round().long(), 0, nb - 1)
+    mag = image_rfft.abs().double()
+    val = mag**2 if do_power_spectrum else mag
+    power = torch.zeros(nb, dtype=torch.float64, device=dev).index_add_(0, idx.flatten(), val.flatten())
     count = torch.zeros(nb, dtype=torch.float64, device=dev).index_add_(
         0, idx.flatten(), torch.ones(idx.numel(), dtype=torch.float64, device=dev))
-    spec = torch.sqrt(power / count.clamp_min(1))
+    spec = power / count.clamp_min(1)
+    if do_power_spectrum:
+        spec = torch.sqrt(spec)
     filt1d = torch.where(spec > 0, 1.0 / spec, torch.zeros_like(spec))
     filt1d = filt1d / filt1d.max()
     ky2, kx2 = rfft_freq_grid(output_shape, device=dev)
     r2 = torch.sqrt(kx2**2 + ky2**2)
-    idx2 = torch.clamp((r2 / 0.5 * (nb - 1)).round().long(), 0, nb - 1)
+    idx2 = torch.clamp((r2 / fmax * (nb - 1)).round().long(), 0, nb - 1)
     return filt1d[idx2].to(torch.float32)
+
+
+def bandpass_filter(shape: tuple[int, int], low: float, high: float, falloff: float, device=None) -> torch.Tensor:
+    """Band [low, high] cycles/pixel on the rfft grid of real ``shape`` with
+    raised-cosine edges of width ``falloff`` (a hard band when falloff = 0);
+    the published form of torch-fourier-filter's bandpass_filter
+    (config/correlation_filters.py:234-271)."""
+    ky, kx = rfft_freq_grid(shape, device=device)
+    r = torch.sqrt(kx**2 + ky**2)
+    f = torch.ones_like(r)
+    if falloff > 0:
+        f = torch.where(r < low, 0.5 * (1 + torch.cos(math.pi * torch.clamp((low - r) / falloff, 0, 1))), f)
+        f = torch.where(r > high, 0.5 * (1 + torch.cos(math.pi * torch.clamp((r - high) / falloff, 0, 1))), f)
+    else:
+        f = ((r >= low) & (r <= high)).to(r.dtype)
+    return f.to(torch.float32)
+
+
+def radial_curve_filter(shape: tuple[int, int], frequencies, amplitudes, device=None) -> torch.Tensor:
+    """A 1-D amplitude curve (cycles/pixel -> amplitude) placed radially on the
+    rfft grid of real ``shape`` by linear interpolation, 1 outside the curve's
+    range (curve_1dim_to_ndim with fill 1, config/correlation_filters.py:290-336)."""
+    f = torch.as_tensor(frequencies, dtype=torch.float64, device=device)
+    a = torch.as_tensor(amplitudes, dtype=torch.float64, device=device)
+    if f.numel() != a.numel() or f.numel() < 1:
+        raise ValueError("frequencies and amplitudes must be non-empty and of equal length")
+    order = torch.argsort(f)
+    f, a = f[order], a[order]
+    ky, kx = rfft_freq_grid(shape, device=device)
+    r = torch.sqrt(kx**2 + ky**2)
+    j = torch.searchsorted(f, r.contiguous()).clamp(1, max(1, f.numel() - 1))
+    if f.numel() == 1:
+        out = torch.where(r == f[0], a[0], torch.ones_like(r))
+    else:
+        f0, f1, a0, a1 = f[j - 1], f[j], a[j - 1], a[j]
+        t = ((r - f0) / (f1 - f0).clamp_min(1e-30)).clamp(0, 1)
+        out = a0 + t * (a1 - a0)
+        out = torch.where((r < f[0]) | (r > f[-1]), torch.ones_like(r), out)
+    return out.to(torch.float32)

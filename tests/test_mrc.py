@@ -53,7 +53,9 @@ def test_result_export_and_load(tmp_path):
     paths = {f"{k}_path": str(tmp_path / f"{k}.mrc") for k in m.MatchTemplateResult.MAPS}
     r = m.MatchTemplateResult(**maps, **paths)
     r.export_results()
-    r2 = m.MatchTemplateResult(**paths)
+    with pytest.raises(ValueError, match="already exists"):  # the reference refuses existing outputs
+        m.MatchTemplateResult(**paths)
+    r2 = m.MatchTemplateResult(**paths, allow_file_overwrite=True)
     r2.load_tensors_from_paths()
     for k in m.MatchTemplateResult.MAPS:
         assert torch.equal(getattr(r2, k), maps[k])
