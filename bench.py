@@ -62,7 +62,7 @@ def _args():
     ap.add_argument("--config", choices=["production", "small", "refbench"], default="production",
                     help="refbench: the reference's published benchmark shape (4096^2, 512^3, 11 defocus)")
     ap.add_argument("--batch", type=int, default=0, help="orientation batch (0: the configuration's)")
-    ap.add_argument("--refine-particles", type=int, default=8)
+    ap.add_argument("--refine-particles", type=int, default=128)
     ap.add_argument("--no-refine", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--refine-plain-only", action="store_true",
@@ -72,8 +72,8 @@ def _args():
                     help="skip timing the reference's torch + cuFFT GPU path on this GPU")
     ap.add_argument("--torch-ref-batches", type=int, default=4)
     ap.add_argument("--torch-ref-streams", type=int, default=4)
-    ap.add_argument("--precision-error-orient", type=int, default=256,
-                    help="orientations of the small configuration checked against the FP64 oracle")
+    ap.add_argument("--precision-error-orient", type=int, default=10240,
+                    help="orientations (uniform random) checked against the FP64 oracle on the small configuration")
     ap.add_argument("--batched-micrographs", type=int, default=12)
     ap.add_argument("--batched-orient", type=int, default=48,
                     help="orientations searched per micrograph in the batched-form sample")
@@ -417,14 +417,18 @@ def precision_bench(args, dev):
             entry["tensor"] = tc
         out[label] = entry
         del s
-    # errors against the FP64 oracle on a prefix of the grid
-    n_err = max(1, min(args.precision_error_orient, N))
+    # errors against the FP64 oracle on args.precision_error_orient orientations
+    # sampled uniformly from SO(3) (seeded), same image and template; the
+    # oracle's torch operations run in FP64 on this GPU
+    n_err = max(1, args.precision_error_orient)
     sub = dict(kw)
-    sub["euler_angles"] = kw["euler_angles"][:n_err]
+    sub["euler_angles"] = sy.random_euler_angles(n_err, seed=2024)
     cpu = {k: v.cpu() for k, v in sub.items()}
-    torch.set_num_threads(os.cpu_count() or 1)
+    t_ref = time.perf_counter()
     ref = orc.core_match_template_cpu(**cpu, orientation_batch_size=32, backend="batched", stat_dtype=torch.float64,
-                                      track_second_best=True, compute_dtype=torch.float64)
+                                      track_second_best=True, compute_dtype=torch.float64, device=dev)
+    t_ref = time.perf_counter() - t_ref
+    torch.cuda.empty_cache()
     mip_r = ref["mip"].double()
     scale = mip_r.abs().clamp_min(1.0)
     sep = (mip_r - ref["second_best"].double()) > 1e-3 * scale
@@ -434,7 +438,8 @@ def precision_bench(args, dev):
         res = s.result(to_cpu=True)
         best = s.best_index.cpu().long()
         out[label]["vs_fp64"] = {
-            "orientations": n_err,
+            "orientations": n_err, "orientation_sample": "uniform random SO(3), seed 2024",
+            "fp64_oracle_s": t_ref,
             "mip_max_rel_err": ((res["mip"].double() - mip_r).abs() / scale).max().item(),
             "argmax_agreement_separated": ((best == ref["best_global_index"].long()) | ~sep).double().mean().item(),
             "argmax_agreement_all": (best == ref["best_global_index"].long()).double().mean().item(),
@@ -568,7 +573,10 @@ def refine_bench(args, dev, with_cpu):
         "mean_refined_snr": float(res["refined_z_score"].mean()),
         "workload": cfg.name,
     }
-    out.update(learned_refine_bench(kw, dev, cfg, res, n))
+    lr = learned_refine_bench(kw, dev, cfg, res, n)
+    out.update(lr)
+    if lr.get("learned"):
+        out["learned_speedup_vs_plain_e2e"] = lr["learned"]["value"] / out["e2e"]
     if with_cpu:
         from oracle import ref_refine_template as orr
 
@@ -587,7 +595,10 @@ def refine_bench(args, dev, with_cpu):
 
 def learned_refine_bench(kw, dev, cfg, plain_res, n_plain):
     """Learned proposals + small local grid (fallback: full plain grid) on the
-    same particles as the plain grid, and its throughput on a larger set."""
+    same particles as the plain grid, and the Gauss-Newton-only ablation (the
+    network's input channels' linearised step, no network) through the same
+    verification and fallback.  Wall-clock particles/s with host tensors in and
+    out, like the plain grid's ``e2e``."""
     from leopard_em_gb300 import proposal as pr
     from leopard_em_gb300 import synthetic as sy
 
@@ -596,30 +607,32 @@ def learned_refine_bench(kw, dev, cfg, plain_res, n_plain):
         return {"learned": None}
     net = pr.ProposalNet(dev)
     pr.load_weights(net, path)
-    # +-0.5 deg at 0.125 deg: the same 576 offsets as +-1 deg at 0.25 deg, measured
-    # higher mean refined SNR than the plain grid (the proposals are within ~0.2 deg)
+    # +-0.5 deg at 0.125 deg: the same 576 offsets as +-1 deg at 0.25 deg, finer
+    # (the proposals are within ~0.2 deg)
     small = sy.local_euler_offsets(0.5, 0.125, 0.5, 0.125)
     small_df = torch.arange(-100.0, 100.0 + 1e-6, 50.0)
-    res, info = pr.refine_with_proposals(net, kw, dev, small, small_df, batch_size=cfg.batch)
-    out = {"learned_mean_refined_snr": float(res["refined_z_score"].mean()),
-           "learned_fallbacks_on_compared": info["fallback"]}
-    n_big = 128
-    kw_big, _ = sy.make_refine_workload(cfg, n_big, device=dev, seed_offset=12345)
-    pr.refine_with_proposals(net, {k: (v[:8] if isinstance(v, torch.Tensor) and v.shape[:1] == (n_big,) else v)
-                                   for k, v in kw_big.items()}, dev, small, small_df, batch_size=cfg.batch)
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    res_big, info_big = pr.refine_with_proposals(net, kw_big, dev, small, small_df, batch_size=cfg.batch)
-    torch.cuda.synchronize(dev)
-    dt = time.perf_counter() - t0
-    out["learned"] = {"metric": "refined particles/s (learned proposal + local grid, full-grid fallback)",
-                      "value": n_big / dt, "unit": "particles/s", "particles": n_big,
-                      "fallbacks": info_big["fallback"],
-                      "correlations_per_particle": info_big["correlations_per_particle"],
-                      "mean_refined_snr": float(res_big["refined_z_score"].mean()),
+    warm = {k: (v[:4] if isinstance(v, torch.Tensor) and v.shape[:1] == (n_plain,) else v) for k, v in kw.items()}
+    pr.refine_with_proposals(net, warm, dev, small, small_df, batch_size=cfg.batch)
+    zp = plain_res["refined_z_score"].double()
+    out = {}
+    for label, which in (("learned", "network"), ("gauss_newton_only", "gauss_newton")):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        res, info = pr.refine_with_proposals(net if which == "network" else None, kw, dev, small, small_df,
+                                             batch_size=cfg.batch, proposal=which)
+        torch.cuda.synchronize(dev)
+        dt = time.perf_counter() - t0
+        z = res["refined_z_score"].double()
+        out[label] = {"metric": "refined particles/s (proposal + local grid, full-grid fallback)",
+                      "proposal": which, "value": n_plain / dt, "unit": "particles/s", "particles": n_plain,
+                      "fallbacks": info["fallback"], "fallback_rate": info["fallback"] / n_plain,
+                      "correlations_per_particle": info["correlations_per_particle"],
+                      "mean_refined_snr": float(z.mean()), "plain_mean_refined_snr": float(zp.mean()),
+                      "snr_at_least_plain": bool(z.mean() >= zp.mean()),
+                      "particles_below_plain": int((z < zp - 1e-6).sum()),
                       "small_grid": "+-0.5 deg @ 0.125 x +-100 A @ 50",
-                      "timing": "wall clock, host tensors in and out (includes network inputs, inference, "
-                                "two refinement calls and any fallback)"}
+                      "timing": "wall clock, host tensors in and out (network inputs, inference, two refinement "
+                                "calls and any fallback)"}
     return out
 
 

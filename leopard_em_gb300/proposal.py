@@ -279,23 +279,33 @@ def predict(net: ProposalNet, inputs: torch.Tensor, batch: int = 1024):
 
 
 # ---- refinement with proposals ------------------------------------------------------
-def refine_with_proposals(net: ProposalNet, kwargs: dict, device, small_offsets: torch.Tensor,
-                          small_defocus: torch.Tensor, batch_size: int = 32, margin: float = 0.0):
+def refine_with_proposals(net: ProposalNet | None, kwargs: dict, device, small_offsets: torch.Tensor,
+                          small_defocus: torch.Tensor, batch_size: int = 32, margin: float = 0.0,
+                          proposal: str = "network"):
     """Proposal -> plain local grid on a small neighbourhood of the proposal;
     the full plain grid is the fallback for every particle whose proposal
     search does not beat the score of its starting pose (all defocus offsets
     of the full grid at the starting orientation).
 
+    ``proposal`` = "network" (the trained CNN) or "gauss_newton" (the
+    linearised step of the network's own input channels, no network: the
+    ablation that measures what the network adds).
+
     Returns (result dict like core_refine_template, info dict)."""
     from .backend.core_refine_template import _ctf_params, core_refine_template
 
+    if proposal not in ("network", "gauss_newton"):
+        raise ValueError(f"proposal must be 'network' or 'gauss_newton', got {proposal!r}")
     dev = torch.device(device)
     ctf = _ctf_params(kwargs["ctf_kwargs"])
     e0 = kwargs["euler_angles"].to(torch.float64)
     r0 = rot.euler_zyz_to_rotmat(e0)
-    x, _ = make_inputs(kwargs["particle_stack_dft"], kwargs["template_dft"], r0.float(), kwargs["defocus_u"],
-                       kwargs["defocus_v"], kwargs["defocus_angle"], ctf, dev)
-    delta, ddf = decode_outputs(predict(net, x))
+    x, gn = make_inputs(kwargs["particle_stack_dft"], kwargs["template_dft"], r0.float(), kwargs["defocus_u"],
+                        kwargs["defocus_v"], kwargs["defocus_angle"], ctf, dev)
+    if proposal == "network":
+        delta, ddf = decode_outputs(predict(net, x))
+    else:
+        delta, ddf = gauss_newton_proposal(gn)
     r_prop = delta.cpu() @ r0
     e_prop = rot.rotmat_to_euler_zyz(r_prop).to(torch.float32)
     prop = dict(kwargs)

@@ -65,6 +65,21 @@ def euler_zyz_from_rotmat(R: np.ndarray) -> np.ndarray:
     return np.array([phi % 360.0, theta, psi % 360.0])
 
 
+def random_euler_angles(n: int, seed: int = 0) -> torch.Tensor:
+    """(n, 3) float32 ZYZ Euler angles (degrees) of rotations drawn uniformly
+    from SO(3) (normalised Gaussian quaternions), seeded."""
+    rng = np.random.default_rng(seed)
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    w, x, y, z = q.T
+    R = np.stack([
+        np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)], -1),
+        np.stack([2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)], -1),
+        np.stack([2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], -1),
+    ], 1)
+    return torch.tensor(np.stack([euler_zyz_from_rotmat(r) for r in R]), dtype=torch.float32)
+
+
 def rotmat_zyz(euler_deg) -> np.ndarray:
     phi, theta, psi = (math.radians(a) for a in euler_deg)
 

@@ -86,13 +86,13 @@ def _trilinear_zero_outside(volume: torch.Tensor, coords: torch.Tensor) -> torch
     """
     shape = volume.shape
     flat = coords.reshape(-1, 3)
-    dims = torch.tensor(shape, dtype=flat.dtype)
+    dims = torch.tensor(shape, dtype=flat.dtype, device=flat.device)
     inside = ((flat >= 0) & (flat <= dims - 1)).all(dim=-1)
     c = torch.minimum(torch.clamp(flat, min=0.0), dims - 1)
     i0 = torch.floor(c).long()
     t = c - i0.to(c.dtype)
     i1 = torch.minimum(i0 + 1, (dims - 1).long())
-    out = torch.zeros(flat.shape[0], dtype=volume.dtype)
+    out = torch.zeros(flat.shape[0], dtype=volume.dtype, device=volume.device)
     for dz in (0, 1):
         iz = i1[:, 0] if dz else i0[:, 0]
         wz = t[:, 0] if dz else 1 - t[:, 0]
@@ -117,15 +117,16 @@ def extract_central_slices_rfft_3d(
     """
     d = volume_rfft.shape[0]
     rdtype = volume_rfft.real.dtype
-    fy = torch.fft.fftshift(torch.fft.fftfreq(d, dtype=rdtype))
-    fx = torch.fft.rfftfreq(d, dtype=rdtype)
+    dev = volume_rfft.device
+    fy = torch.fft.fftshift(torch.fft.fftfreq(d, dtype=rdtype, device=dev))
+    fx = torch.fft.rfftfreq(d, dtype=rdtype, device=dev)
     gy, gx = torch.meshgrid(fy, fx, indexing="ij")
     zyx = torch.stack([torch.zeros_like(gy), gy, gx], dim=-1)  # (d, wc, 3)
-    r_zyx = torch.flip(rotation_matrices.to(rdtype), dims=(-2, -1))
+    r_zyx = torch.flip(rotation_matrices.to(dev, rdtype), dims=(-2, -1))
     rot = torch.einsum("...ij,hwj->...hwi", r_zyx, zyx)
     conj = rot[..., 2] < 0
     rot = torch.where(conj[..., None], -rot, rot)
-    dc = torch.tensor([d // 2, d // 2, 0], dtype=rdtype)
+    dc = torch.tensor([d // 2, d // 2, 0], dtype=rdtype, device=dev)
     coords = rot * d + dc
     samples = _trilinear_zero_outside(volume_rfft, coords)
     return torch.where(conj, samples.conj(), samples)
@@ -168,7 +169,7 @@ def cross_correlate_streamed(image_dft, template_dft, rotation_matrices, project
     img_shape = (image_dft.shape[0], image_dft.shape[1] * 2 - 2)
     n_o = rotation_matrices.shape[0]
     n_cs, n_df = projective_filters.shape[0], projective_filters.shape[1]
-    out = torch.empty((n_cs, n_df, n_o, *img_shape), dtype=image_dft.real.dtype)
+    out = torch.empty((n_cs, n_df, n_o, *img_shape), dtype=image_dft.real.dtype, device=image_dft.device)
     fs_all = prepare_fourier_slices(template_dft, rotation_matrices)
     for i in range(n_o):
         for j in range(n_df):
@@ -250,43 +251,48 @@ def scale_mip(mip, correlation_sum, correlation_squared_sum, total_correlation_p
 def core_match_template_cpu(
     image_dft, template_dft, ctf_filters, whitening_filter_template, defocus_values,
     pixel_values, euler_angles, orientation_batch_size=1, backend="streamed",
-    stat_dtype=torch.float32, track_second_best=False, compute_dtype=torch.float32,
+    stat_dtype=torch.float32, track_second_best=False, compute_dtype=torch.float32, device=None,
 ):
     """CPU restatement of ``core_match_template`` (core_match_template.py:146-363).
 
     ``stat_dtype`` float32 reproduces the reference's statistics accumulation
     (``DEFAULT_STATISTIC_DTYPE``, :31); float64 gives the FP64 oracle.
     ``compute_dtype`` float64 runs the whole correlation in double precision.
+    ``device`` runs the same torch operations elsewhere (a CUDA device makes an
+    FP64 oracle of many orientations affordable); results come back on the CPU.
     The last partial orientation batch gets exactly as many global indices as it
     has orientations (the reference always generates a full batch, :513-520).
     """
+    dev = torch.device(device) if device is not None else torch.device("cpu")
     cdt = torch.complex128 if compute_dtype == torch.float64 else torch.complex64
-    image_dft = image_dft.to(cdt)
-    template_dft = template_dft.to(cdt)
-    pf = (ctf_filters * whitening_filter_template[None, None, ...]).to(compute_dtype)
+    image_dft = image_dft.to(dev, cdt)
+    template_dft = template_dft.to(dev, cdt)
+    pf = (ctf_filters.to(dev) * whitening_filter_template.to(dev)[None, None, ...]).to(compute_dtype)
     euler_angles = euler_angles.to(torch.float32)
     n_o, n_df, n_cs = euler_angles.shape[0], defocus_values.shape[0], pixel_values.shape[0]
     total = n_o * n_df * n_cs
     img_shape = (image_dft.shape[0], image_dft.shape[1] * 2 - 2)
     incr = torch.tensor(
-        [df * n_o + cs * n_df * n_o for cs in range(n_cs) for df in range(n_df)], dtype=torch.int64
+        [df * n_o + cs * n_df * n_o for cs in range(n_cs) for df in range(n_df)], dtype=torch.int64, device=dev
     )
-    mip = torch.full(img_shape, -float("inf"), dtype=compute_dtype)
-    best = torch.full(img_shape, -1, dtype=torch.int64)
-    s1 = torch.zeros(img_shape, dtype=stat_dtype)
-    s2 = torch.zeros(img_shape, dtype=stat_dtype)
-    second = torch.full(img_shape, -float("inf"), dtype=compute_dtype) if track_second_best else None
+    mip = torch.full(img_shape, -float("inf"), dtype=compute_dtype, device=dev)
+    best = torch.full(img_shape, -1, dtype=torch.int64, device=dev)
+    s1 = torch.zeros(img_shape, dtype=stat_dtype, device=dev)
+    s2 = torch.zeros(img_shape, dtype=stat_dtype, device=dev)
+    second = torch.full(img_shape, -float("inf"), dtype=compute_dtype, device=dev) if track_second_best else None
     B = orientation_batch_size
     for i in range(0, n_o, B):
         eb = euler_angles[i : i + B]
-        rot = euler_to_rotmat_zyz(eb, dtype=compute_dtype)
-        idx = torch.arange(i, i + eb.shape[0], dtype=torch.int64)
+        rot = euler_to_rotmat_zyz(eb, dtype=compute_dtype).to(dev)
+        idx = torch.arange(i, i + eb.shape[0], dtype=torch.int64, device=dev)
         bsi = (idx + incr[:, None]).flatten()
         if backend == "batched":
             cc = cross_correlate_batched_cpu(image_dft, template_dft, rot, pf)
         else:
             cc = cross_correlate_streamed(image_dft, template_dft, rot, pf)
         iteration_statistics_update(cc, bsi, mip, best, s1, s2, img_shape[0], img_shape[1], second)
+    best, mip, s1, s2 = best.cpu(), mip.cpu(), s1.cpu(), s2.cpu()
+    second = second.cpu() if second is not None else None
     phi, theta, psi, dfv = decode_global_search_index(best, pixel_values, defocus_values, euler_angles)
     mip, scaled, mean, std = scale_mip(mip, s1, s2, total)
     out = {
