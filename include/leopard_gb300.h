@@ -342,6 +342,53 @@ int lgb_tc_gemm(int m_tiles, int n_tiles, int k_chunks, int bn, int f16, int ter
                 int* err, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Pre-processing of the search inputs (once per micrograph).                */
+/* ------------------------------------------------------------------------ */
+
+/* CTF filter stack of one optics group, out float32 (device)
+ * [n_pixel_sizes][n_defocus][d][d/2+1] on the unshifted rfft grid of a d x d
+ * template: -sin(chi) exp(-B k^2 / 4) with defocus (defocus_u + defocus_v)/2 +
+ * offset, astigmatism |defocus_u - defocus_v|/2 at astigmatism_angle_deg, and
+ * Cs scaled for the pixel-size offsets, FP64 arithmetic.  Replaces
+ * calculate_ctf_filter_stack (utils/ctf_utils.py:19-116, torch-ctf's
+ * calculate_ctf_2d with torch-fourier-filter's b_envelope). */
+int lgb_ctf_filter_stack(int template_size, double defocus_u, double defocus_v, double astigmatism_angle_deg,
+                         const lgb_ctf_params* ctf, const float* defocus_offsets, int n_defocus,
+                         const float* pixel_size_offsets, int n_pixel_sizes, float* out, void* stream);
+
+/* Radially binned spectrum of n_images rfft images (complex64 device
+ * [n][H][W/2+1]): bin of |k| = round(|k| / max_freq * (n_bins - 1)) clamped
+ * to the last bin (|k| in cycles/pixel); bin_sum[n][n_bins] = sum of |F|^2
+ * (power = 1) or |F| (power = 0), bin_count[n][n_bins] = samples (FP64,
+ * device).  First half of the whitening filter of
+ * correlation_filters.py:49-108 (torch-fourier-filter's whitening_filter). */
+int lgb_radial_spectrum(int n_images, int image_h, int image_w, const void* image_dft, int n_bins, double max_freq,
+                        int power, double* bin_sum, double* bin_count, void* stream);
+
+/* Second half: per image the 1-D filter 1/spectrum (square root of the mean
+ * power when power = 1), 0 where the spectrum is 0, normalised to maximum 1
+ * (written over bin_sum), sampled by nearest bin onto the rfft grid of an
+ * out_h x out_w real image: out float32 [n][out_h][out_w/2+1] (device). */
+int lgb_whitening_filter(int n_images, int n_bins, double max_freq, int power, double* bin_sum,
+                         const double* bin_count, int out_h, int out_w, float* out, void* stream);
+
+/* Bandpass [low, high] cycles/pixel with raised-cosine edges of width falloff
+ * (a hard band when 0) on the rfft grid of an h x w real image, out float32
+ * [h][w/2+1] (device).  Replaces BandpassFilterConfig.calculate_bandpass_filter
+ * (correlation_filters.py:234-271). */
+int lgb_bandpass_filter(int h, int w, double low, double high, double falloff, float* out, void* stream);
+
+/* out[n] = F[n] f[n] / sqrt(P[n]) * sqrt(D) * sqrt(area_ratio), where P[n] =
+ * sum |F f|^2 with interior rfft columns counted twice, D the same weighted sum
+ * of the bandpass filter and area_ratio = (image area) / (box area).  F, out
+ * complex64 [n][H][W/2+1]; filters float32, image n at filters + n *
+ * filter_stride (0: one filter for all); scratch >= n_images + 1 doubles
+ * (device).  Replaces preprocess_image (utils/image_processing.py:16-75). */
+int lgb_preprocess_image(int n_images, int image_h, int image_w, const void* image_dft, const float* filters,
+                         long long filter_stride, const float* bandpass, double area_ratio, double* scratch,
+                         void* out, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Refinement proposal network (no reference counterpart: Leopard-EM has no  */
 /* learned component; closest analogue core_differentiable_refine.py).       */
 /* Activations and forward weights are BF16 (device), accumulation FP32,     */

@@ -110,6 +110,12 @@ _SIGNATURES = {
     "lgb_peaks_find": ([_I, _I, _P, ctypes.c_float, ctypes.c_float, _I, _P, _SZ, _I, _P,
                         ctypes.POINTER(_I), ctypes.POINTER(_I), _P], _I),
     "lgb_wait_timeout_selftest": ([ctypes.c_uint, _P, _P], _I),
+    "lgb_ctf_filter_stack": ([_I, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.POINTER(CtfParams), _P, _I,
+                              _P, _I, _P, _P], _I),
+    "lgb_radial_spectrum": ([_I, _I, _I, _P, _I, ctypes.c_double, _I, _P, _P, _P], _I),
+    "lgb_whitening_filter": ([_I, _I, ctypes.c_double, _I, _P, _P, _I, _I, _P, _P], _I),
+    "lgb_bandpass_filter": ([_I, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double, _P, _P], _I),
+    "lgb_preprocess_image": ([_I, _I, _I, _P, _P, _LL, _P, ctypes.c_double, _P, _P, _P], _I),
     "lgb_tc_gemm": ([_I] * 6 + [_P] * 5 + [_I, _I, _I, _P, _P], _I),
     "lgb_nn_conv3x3_forward": ([_I] * 7 + [_P] * 4 + [_P], _I),
     "lgb_nn_conv3x3_backward": ([_I] * 6 + [_P] * 6 + [_P], _I),

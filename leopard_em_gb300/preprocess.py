@@ -11,7 +11,10 @@ does before calling the backend (match_template_manager.py:140-218):
   * ``whitening_filter``              a radially averaged 1/sqrt(power) filter,
     the published construction of torch-fourier-filter's whitening_filter.
 They are not part of the timed search.  Every function works on the device
-of its input tensors (CPU or CUDA).
+of its input tensors: on a CUDA device the CTF stack, the whitening and
+bandpass filters and the filter-and-normalise step run as this package's
+kernels (``csrc/preprocess.cu``); on the CPU they run as torch operations.
+The image and template rffts are torch.fft on either device.
 """
 
 from __future__ import annotations
@@ -19,6 +22,16 @@ from __future__ import annotations
 import math
 
 import torch
+
+
+def _on_cuda(device) -> bool:
+    return device is not None and torch.device(device).type == "cuda"
+
+
+def _native():
+    from . import _native as nat
+
+    return nat
 
 
 def volume_to_rfft_fourier_slice(volume: torch.Tensor) -> torch.Tensor:
@@ -32,6 +45,9 @@ def volume_to_rfft_fourier_slice(volume: torch.Tensor) -> torch.Tensor:
 
 def preprocess_image(image_rfft, cumulative_fourier_filters, bandpass_filter, full_image_shape, extracted_box_shape):
     """Filter, normalise to unit power, scale by sqrt(dimensionality) and box area."""
+    if image_rfft.is_cuda:
+        return _preprocess_image_native(image_rfft, cumulative_fourier_filters, bandpass_filter, full_image_shape,
+                                        extracted_box_shape)
     image_rfft = image_rfft * cumulative_fourier_filters
     sq = torch.abs(image_rfft) ** 2
     ssum = torch.sum(sq, dim=(-2, -1), keepdim=True)
@@ -42,6 +58,33 @@ def preprocess_image(image_rfft, cumulative_fourier_filters, bandpass_filter, fu
     img_h, img_w = full_image_shape
     box_h, box_w = extracted_box_shape
     return image_rfft * ((img_h * img_w) / (box_h * box_w)) ** 0.5
+
+
+def _preprocess_image_native(image_rfft, filters, bandpass, full_image_shape, extracted_box_shape):
+    import ctypes
+
+    nat = _native()
+    dev = image_rfft.device
+    H, wc = image_rfft.shape[-2:]
+    n = 1 if image_rfft.dim() == 2 else int(image_rfft.shape[0])
+    F = image_rfft.to(torch.complex64).reshape(n, H, wc).contiguous()
+    f = filters.to(dev, torch.float32)
+    if f.dim() == 3 and f.shape[0] == n and n > 1:
+        f = f.contiguous()
+        stride = H * wc
+    else:
+        f = f.reshape(H, wc).contiguous()
+        stride = 0
+    bp = bandpass.to(dev, torch.float32).reshape(H, wc).contiguous()
+    out = torch.empty_like(F)
+    scratch = torch.empty(n + 1, dtype=torch.float64, device=dev)
+    (ih, iw), (bh, bw) = full_image_shape, extracted_box_shape
+    with torch.cuda.device(dev):
+        s = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        nat.check(nat.lib().lgb_preprocess_image(n, H, 2 * (wc - 1), F.data_ptr(), f.data_ptr(), stride,
+                                                 bp.data_ptr(), float(ih * iw) / float(bh * bw),
+                                                 scratch.data_ptr(), out.data_ptr(), s), "preprocess_image")
+    return out.reshape(image_rfft.shape)
 
 
 def rfft_freq_grid(shape: tuple[int, int], pixel_size: float = 1.0, device=None):
@@ -114,6 +157,10 @@ def ctf_filter_stack(
     device=None,
 ) -> torch.Tensor:
     """(num_pixel_sizes, num_defocus, d, d//2+1) stack as ctf_utils.py:19-116."""
+    if _on_cuda(device):
+        return _ctf_filter_stack_native(template_size, defocus_u, defocus_v, defocus_offsets, pixel_size_offsets,
+                                        astigmatism_angle, voltage, spherical_aberration, amplitude_contrast,
+                                        phase_shift, pixel_size, b_factor, torch.device(device))
     mean_df = (defocus_u + defocus_v) / 2
     astig = abs(defocus_u - defocus_v) / 2
     cs_values = get_cs_range(pixel_size, pixel_size_offsets, spherical_aberration)
@@ -129,6 +176,46 @@ def ctf_filter_stack(
             )
         )
     return torch.stack(stack)
+
+
+def _ctf_filter_stack_native(d, du, dv, dfo, pxo, ang, voltage, cs, amp, phase, px, b, dev):
+    import ctypes
+
+    nat = _native()
+    dfo = torch.as_tensor(dfo, dtype=torch.float32).reshape(-1).to(dev).contiguous()
+    pxo = torch.as_tensor(pxo, dtype=torch.float32).reshape(-1).to(dev).contiguous()
+    out = torch.empty((pxo.numel(), dfo.numel(), d, d // 2 + 1), dtype=torch.float32, device=dev)
+    prm = nat.CtfParams(voltage_kv=float(voltage), spherical_aberration_mm=float(cs),
+                        amplitude_contrast=float(amp), b_factor=float(b), phase_shift_deg=float(phase),
+                        pixel_size=float(px))
+    with torch.cuda.device(dev):
+        s = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        nat.check(nat.lib().lgb_ctf_filter_stack(int(d), float(du), float(dv), float(ang), ctypes.byref(prm),
+                                                 dfo.data_ptr(), dfo.numel(), pxo.data_ptr(), pxo.numel(),
+                                                 out.data_ptr(), s), "ctf_filter_stack")
+    return out
+
+
+def _whitening_filter_native(image_rfft, output_shape, nb, fmax, power):
+    import ctypes
+
+    nat = _native()
+    dev = image_rfft.device
+    H, wc = image_rfft.shape[-2:]
+    n = 1 if image_rfft.dim() == 2 else int(image_rfft.shape[0])
+    F = image_rfft.to(torch.complex64).reshape(n, H, wc).contiguous()
+    bsum = torch.empty((n, nb), dtype=torch.float64, device=dev)
+    bcnt = torch.empty((n, nb), dtype=torch.float64, device=dev)
+    oh, ow = output_shape
+    out = torch.empty((n, oh, ow // 2 + 1), dtype=torch.float32, device=dev)
+    with torch.cuda.device(dev):
+        s = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        L = nat.lib()
+        nat.check(L.lgb_radial_spectrum(n, H, 2 * (wc - 1), F.data_ptr(), nb, float(fmax), int(power),
+                                        bsum.data_ptr(), bcnt.data_ptr(), s), "radial_spectrum")
+        nat.check(L.lgb_whitening_filter(n, nb, float(fmax), int(power), bsum.data_ptr(), bcnt.data_ptr(), oh, ow,
+                                         out.data_ptr(), s), "whitening_filter")
+    return out[0] if image_rfft.dim() == 2 else out
 
 
 def whitening_filter(image_rfft: torch.Tensor, output_shape: tuple[int, int], num_bins: int | None = None,
@@ -147,9 +234,11 @@ def whitening_filter(image_rfft: torch.Tensor, output_shape: tuple[int, int], nu
     fmax = 0.5 if max_freq is None else float(max_freq)
     if fmax <= 0:
         raise ValueError("max_freq must be > 0")
+    nb = num_bins or int(max(H, W) // 2 + 1)
+    if image_rfft.is_cuda:
+        return _whitening_filter_native(image_rfft, tuple(output_shape), nb, fmax, do_power_spectrum)
     ky, kx = rfft_freq_grid((H, W), device=dev)
     r = torch.sqrt(kx**2 + ky**2)
-    nb = num_bins or int(max(H, W) // 2 + 1)
     idx = torch.clamp((r / fmax * (nb - 1)).round().long(), 0, nb - 1)
     mag = image_rfft.abs().double()
     val = mag**2 if do_power_spectrum else mag
@@ -172,6 +261,18 @@ def bandpass_filter(shape: tuple[int, int], low: float, high: float, falloff: fl
     raised-cosine edges of width ``falloff`` (a hard band when falloff = 0);
     the published form of torch-fourier-filter's bandpass_filter
     (config/correlation_filters.py:234-271)."""
+    if _on_cuda(device):
+        import ctypes
+
+        nat = _native()
+        dev = torch.device(device)
+        h, w = shape
+        out = torch.empty((h, w // 2 + 1), dtype=torch.float32, device=dev)
+        with torch.cuda.device(dev):
+            s = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+            nat.check(nat.lib().lgb_bandpass_filter(int(h), int(w), float(low), float(high), float(falloff),
+                                                    out.data_ptr(), s), "bandpass_filter")
+        return out
     ky, kx = rfft_freq_grid(shape, device=device)
     r = torch.sqrt(kx**2 + ky**2)
     f = torch.ones_like(r)

@@ -34,6 +34,10 @@ gaussian_noise_zscore_cutoff) and ``analysis/utils.py``
 (filter_peaks_by_distance); ``pandas`` (imported by the package's
 match_template_peaks.py, unused here) is a stand-in module.
 
+``tests/golden/preprocess_small.npz`` (``--preprocess``): the reference's
+``preprocess_image`` (utils/image_processing.py:16-75) and its CTF-stack
+wrapper (utils/ctf_utils.py:19-116) with the stand-ins above for torch_ctf.
+
 ``tests/golden/xcorr_small.npz`` (``--xcorr``): the reference's
 ``cross_correlate_particle_stack`` (backend/core_refine_template.py:771-895)
 on small stacks, both modes, with the stand-ins above for the slice extraction.
@@ -377,6 +381,63 @@ def _refine_golden(ref_root):
     np.savez_compressed(path, **out)
     print("wrote", path, os.path.getsize(path), "bytes")
 
+
+def main_preprocess(ref_root):
+    """preprocess_image (utils/image_processing.py:16-75) and the CTF-stack
+    wrapper calculate_ctf_filter_stack_full_args (utils/ctf_utils.py:19-116)
+    from the reference's own code -> preprocess_small.npz.  torch_ctf /
+    b_envelope are the stand-ins above (the oracle's restatements), so the CTF
+    case pins the wrapper's defocus / astigmatism / Cs / envelope handling."""
+    _install_stubs()
+    dw = types.ModuleType("torch_fourier_filter.dose_weight")
+
+    def _no_dose(*a, **k):
+        raise NotImplementedError("dose weighting is not used by the golden cases")
+
+    dw.dose_weight_movie = _no_dose
+    sys.modules["torch_fourier_filter.dose_weight"] = dw
+    for name in ("leopard_em", "leopard_em.utils"):
+        sys.modules.setdefault(name, types.ModuleType(name))
+    _load(ref_root, "utils/search_utils.py", "leopard_em.utils.search_utils")
+    ip = _load(ref_root, "utils/image_processing.py", "leopard_em_ref_image_processing")
+    cu = _load(ref_root, "utils/ctf_utils.py", "leopard_em_ref_ctf_utils")
+    g = torch.Generator().manual_seed(77)
+    out = {}
+    # one micrograph-like spectrum, filter and bandpass
+    img = torch.fft.rfftn(torch.randn(96, 128, generator=g))
+    img[0, 0] = 0
+    filt = (torch.rand(96, 65, generator=g) + 0.25).to(torch.float32)
+    band = (torch.rand(96, 65, generator=g) > 0.2).to(torch.float32)
+    out["single/image_dft"] = img.numpy()
+    out["single/filter"] = filt.numpy()
+    out["single/bandpass"] = band.numpy()
+    out["single/out"] = ip.preprocess_image(img, filt, band, (96, 128), (96, 128)).numpy()
+    # a particle stack: per-image filters, box area smaller than the image's
+    stack = torch.fft.rfftn(torch.randn(3, 64, 64, generator=g), dim=(-2, -1))
+    filts = (torch.rand(3, 64, 33, generator=g) + 0.1).to(torch.float32)
+    band2 = torch.ones(64, 33)
+    out["stack/image_dft"] = stack.numpy()
+    out["stack/filter"] = filts.numpy()
+    out["stack/bandpass"] = band2.numpy()
+    out["stack/out"] = ip.preprocess_image(stack, filts, band2, (64, 64), (49, 49)).numpy()
+    # CTF filter stack: astigmatic, B envelope, two pixel sizes, three defocus planes
+    kw = dict(astigmatism_angle=25.0, voltage=300.0, spherical_aberration=2.7, amplitude_contrast_ratio=0.07,
+              ctf_B_factor=60.0, phase_shift=0.0, pixel_size=1.06, even_zernikes=None, odd_zernikes=None,
+              mag_matrix=None)
+    dfo = torch.tensor([-200.0, 0.0, 200.0])
+    pxo = torch.tensor([-0.02, 0.02])
+    ctf = cu.calculate_ctf_filter_stack_full_args((32, 32), 5200.0, 4950.0, dfo, pxo, **kw)
+    out["ctf/out"] = ctf.numpy()
+    out["ctf/defocus_offsets"] = dfo.numpy()
+    out["ctf/pixel_size_offsets"] = pxo.numpy()
+    path = os.path.join(HERE, "preprocess_small.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__" and "--preprocess" in sys.argv:
+    main_preprocess([a for a in sys.argv[1:] if a != "--preprocess"][0])
+    sys.exit(0)
 
 if __name__ == "__main__" and "--xcorr" in sys.argv:
     main_xcorr([a for a in sys.argv[1:] if a != "--xcorr"][0])
