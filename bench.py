@@ -489,7 +489,8 @@ def batched_bench(args, dev):
                       "cross_correlations_per_s": len(mics) * n * n_cd / (sum(rep.ms) / 1e3)}
         if tune:
             out[label]["tuning"] = {f"{g[0]}x{g[1]}": {"orientation_batch": t.orientation_batch,
-                                                        "col_waves": t.col_waves, "graph_batches": t.graph_batches}
+                                                        "col_waves": t.col_waves, "graph_batches": t.graph_batches,
+                                                        "transposed": bool(t.transpose)}
                                     for g, t in zip(rep.grids, rep.tunings)}
             out[label]["grids"] = [list(g) for g in rep.grids]
     best = out["tuned_graph"]

@@ -1,7 +1,10 @@
 """Autotuner for the launch parameters of the whole-orientation search.
 
-Three choices change the speed of ``lgb_match_search`` but not its results at
-valid positions: the correlation grid (the FFT lengths; a micrograph may be
+Four choices change the speed of ``lgb_match_search`` but not its results at
+valid positions (beyond rounding): the orientation of the search (a
+transposed micrograph puts its width on the column transform, which pays when
+the height has only a slow column kernel, e.g. 5760 rows), the correlation
+grid (the FFT lengths; a micrograph may be
 zero padded past the smallest compiled grid to a power of two, whose
 transforms have the register-fused kernels), the orientation batch B
 (correlograms per statistics update: larger batches amortise the
@@ -42,6 +45,7 @@ class SearchTuning:
     ms_per_orientation: float
     grid_h: int = 0  # 0: the smallest compiled grid
     grid_w: int = 0
+    transpose: bool = False  # search the transposed micrograph (grid is then the transposed grid)
 
     @property
     def grid(self):
@@ -126,8 +130,10 @@ def tune_search(image_dft, template_dft, ctf_filters, whitening_filter_template,
     W = 2 * (wc - 1)
     d = int(template_dft.shape[0])
     C, D = int(pixel_values.shape[0]), int(defocus_values.shape[0])
-    grids = grid_candidates(H, W) if tune_grid else [padded_grid(H, W)]
-    key = tuning_key(dev, grids[0], (H, W), d, C, D) + ("/grid" if tune_grid else "")
+    grids = [(g, False) for g in (grid_candidates(H, W) if tune_grid else [padded_grid(H, W)])]
+    if tune_grid and H != W and H % 2 == 0:
+        grids += [(g, True) for g in grid_candidates(W, H)]
+    key = tuning_key(dev, grids[0][0], (H, W), d, C, D) + ("/grid+T" if tune_grid else "")
     path = cache_path()
     if use_cache:
         hit = _load_cache(path).get(key)
@@ -147,11 +153,14 @@ def tune_search(image_dft, template_dft, ctf_filters, whitening_filter_template,
         free = torch.cuda.mem_get_info(dev)[0]
 
         def make_search(cand):
-            g, b, w = cand
-            return MatchTemplateSearch(**inputs, device=dev, orientation_batch_size=b, col_waves=w, grid=g)
+            (g, tr), b, w = cand
+            return MatchTemplateSearch(**inputs, device=dev, orientation_batch_size=b, col_waves=w, grid=g,
+                                       transpose=tr)
 
-        def fits(g, b):
-            p = MatchProblem(g[0], g[1], d, C, D, n_probe, b, H, W, 0)
+        def fits(gt, b):
+            g, tr = gt
+            mh, mw = (W, H) if tr else (H, W)
+            p = MatchProblem(g[0], g[1], d, C, D, n_probe, b, mh, mw, 0)
             need = ctypes.c_size_t(0)
             if lib().lgb_match_workspace_size(ctypes.byref(p), ctypes.byref(need)) != 0:
                 return False
@@ -174,7 +183,7 @@ def tune_search(image_dft, template_dft, ctf_filters, whitening_filter_template,
         ms = timings[(best_g, best_b, best_w)]
     tuning = SearchTuning(orientation_batch=best_b, col_waves=best_w,
                           graph_batches=SearchTuning.graph_batches_for(best_b), ms_per_orientation=float(ms),
-                          grid_h=best_g[0], grid_w=best_g[1])
+                          grid_h=best_g[0][0], grid_w=best_g[0][1], transpose=best_g[1])
     if use_cache:
         _store_cache(path, key, asdict(tuning))
     return tuning

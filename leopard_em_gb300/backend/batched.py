@@ -8,7 +8,9 @@ next compiled FFT lengths, or a larger compiled grid whose transforms are
 faster, zero padded), with the grid, orientation batch and column split chosen
 by the autotuner (cached per shape, so micrographs of a repeated size reuse
 the choice), and the orientation batches replayed as CUDA graphs
-(``lgb_match_search_graph``).
+(``lgb_match_search_graph``).  A micrograph whose height has only a slow
+column transform may run transposed (the autotuner times both orientations;
+``core_match_template.transposed_template_dft``).
 The host enqueues everything without waiting; per-micrograph device times come
 from CUDA events between micrographs.
 """
@@ -20,7 +22,8 @@ from dataclasses import dataclass, field
 import torch
 
 from .. import autotune
-from .core_match_template import MatchTemplateSearch, _single_cuda_device, padded_grid
+from .core_match_template import (MatchTemplateSearch, _single_cuda_device, padded_grid, transposed_euler_angles,
+                                  transposed_template_dft)
 
 PER_MICROGRAPH_KEYS = ("image_dft", "ctf_filters", "whitening_filter_template", "defocus_values", "pixel_values")
 
@@ -71,6 +74,7 @@ def match_template_batch(micrographs, template_dft, euler_angles, device, orient
         eul = euler_angles.to(dev, torch.float32).contiguous()
         events = []
         pending = []
+        tdft_t = eul_t = None  # template and rotations of the transposed frame, made once
         for m in micrographs:
             H, wc = m["image_dft"].shape
             if tune:
@@ -79,7 +83,11 @@ def match_template_batch(micrographs, template_dft, euler_angles, device, orient
             else:
                 b = int(orientation_batch_size)
                 t = autotune.SearchTuning(b, 0, autotune.SearchTuning.graph_batches_for(b), float("nan"))
-            grid = t.grid or padded_grid(H, 2 * (wc - 1))
+            tr = bool(getattr(t, "transpose", False))
+            grid = t.grid or (padded_grid(2 * (wc - 1), H) if tr else padded_grid(H, 2 * (wc - 1)))
+            if tr and tdft_t is None:
+                tdft_t = transposed_template_dft(tdft)
+                eul_t = transposed_euler_angles(eul).to(dev)
             a = torch.cuda.Event(enable_timing=True)
             z = torch.cuda.Event(enable_timing=True)
             a.record(stream)
@@ -87,7 +95,8 @@ def match_template_batch(micrographs, template_dft, euler_angles, device, orient
                                          m["defocus_values"], m["pixel_values"], eul, dev,
                                          orientation_batch_size=t.orientation_batch,
                                          graph_batches=t.graph_batches if use_graphs else 0, col_waves=t.col_waves,
-                                         grid=grid)
+                                         grid=grid, transpose=tr, transposed_template=tdft_t if tr else None,
+                                         transposed_euler=eul_t if tr else None)
             search.run(begin, end)
             res = search.result(to_cpu=False)
             z.record(stream)

@@ -88,6 +88,78 @@ def padded_grid(h: int, w: int) -> tuple[int, int]:
     return hp, wp
 
 
+# ---------------------------------------------------------------------------
+# Transposed search.  Searching the transposed micrograph I^T with the template
+# volume's x and y axes swapped and every rotation conjugated by that swap
+# (R' = S R S, S the x <-> y exchange; a proper rotation again) yields the
+# transposed correlograms: the projection of the swapped volume at R' is the
+# transposed projection at R, and the cross-correlation of transposed images
+# is the transposed cross-correlation.  The statistics maps of the transposed
+# search are the transposed maps of the direct search (the orientation index
+# of every correlogram is unchanged), so a micrograph whose height has only a
+# slow column transform (e.g. 5760) can run on the fused kernels of its width.
+# ---------------------------------------------------------------------------
+_SWAP_XY = torch.tensor([[0.0, 1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]], dtype=torch.float64)
+
+
+def _rotmat_to_euler_zyz_robust(R: torch.Tensor) -> torch.Tensor:
+    """ZYZ Euler angles (degrees) of rotations (N, 3, 3), FP64, including
+    theta = 0 and 180 (psi = 0 there, phi carries the whole z rotation)."""
+    R = R.to(torch.float64)
+    theta = torch.acos(torch.clamp(R[:, 2, 2], -1.0, 1.0))
+    st = torch.sqrt(R[:, 0, 2] ** 2 + R[:, 1, 2] ** 2)
+    regular = st > 1e-9
+    phi = torch.where(regular, torch.atan2(R[:, 1, 2], R[:, 0, 2]), torch.zeros_like(theta))
+    psi = torch.where(regular, torch.atan2(R[:, 2, 1], -R[:, 2, 0]), torch.zeros_like(theta))
+    # theta = 0: R = Rz(phi + psi); theta = pi: R = Rz(phi) diag(-1, 1, -1) Rz(psi)
+    top = R[:, 2, 2] > 0
+    phi_sing = torch.where(top, torch.atan2(R[:, 1, 0], R[:, 0, 0]), torch.atan2(-R[:, 1, 0], -R[:, 0, 0]))
+    phi = torch.where(regular, phi, phi_sing)
+    return torch.rad2deg(torch.stack([phi, theta, psi], dim=1))
+
+
+def transposed_euler_angles(euler_angles: torch.Tensor) -> torch.Tensor:
+    """Euler angles of S R S for every orientation (float32)."""
+    from ..rotations import euler_zyz_to_rotmat
+
+    R = euler_zyz_to_rotmat(euler_angles.detach().cpu().to(torch.float64))
+    S = _SWAP_XY
+    return _rotmat_to_euler_zyz_robust(S @ R @ S).to(torch.float32)
+
+
+def transposed_half_filter(f: torch.Tensor) -> torch.Tensor:
+    """A real, Hermitian-even filter (..., d, d//2+1) on the rfft grid, as seen
+    in the transposed frame: f'(ky, kx) = f(kx, ky), completing the negative
+    kx half by f(-k) = f(k)."""
+    d = f.shape[-2]
+    i = torch.arange(d, device=f.device)[:, None]
+    j = torch.arange(d // 2 + 1, device=f.device)[None, :]
+    low = i <= d // 2
+    rows = torch.where(low, j, (d - j) % d)
+    cols = torch.where(low, i, d - i).expand_as(rows)
+    return f[..., rows, cols].contiguous()
+
+
+def transposed_template_dft(template_dft: torch.Tensor) -> torch.Tensor:
+    """Template spectrum (fftshifted rfft layout, d x d x d//2+1) of the volume
+    with its x and y axes exchanged."""
+    d = template_dft.shape[0]
+    v = torch.fft.irfftn(torch.fft.ifftshift(template_dft.to(torch.complex64), dim=(0, 1)), s=(d, d, d))
+    v = torch.fft.ifftshift(v, dim=(0, 1, 2)).transpose(1, 2).contiguous()
+    t = torch.fft.rfftn(torch.fft.fftshift(v, dim=(0, 1, 2)), dim=(0, 1, 2))
+    return torch.fft.fftshift(t, dim=(0, 1)).contiguous()
+
+
+def transposed_image_dft(image_dft: torch.Tensor) -> torch.Tensor:
+    """rfft of the transposed micrograph (H x W -> W x H; H must be even)."""
+    H, wc = image_dft.shape
+    W = 2 * (wc - 1)
+    if H % 2:
+        raise ValueError("a transposed search needs an even micrograph height")
+    img = torch.fft.irfftn(image_dft.to(torch.complex64), s=(H, W))
+    return torch.fft.rfftn(img.transpose(0, 1).contiguous()).contiguous()
+
+
 class MatchTemplateSearch:
     """Device state of one whole-orientation search over one micrograph.
 
@@ -112,6 +184,9 @@ class MatchTemplateSearch:
         col_waves: int = 0,
         grid: tuple[int, int] | None = None,
         precision: str = "fp32",
+        transpose: bool = False,
+        transposed_template: torch.Tensor | None = None,
+        transposed_euler: torch.Tensor | None = None,
     ):
         """``graph_batches`` > 0 replays that many orientation batches per CUDA
         graph launch (``lgb_match_search_graph``); ``col_waves`` sets the column
@@ -121,8 +196,29 @@ class MatchTemplateSearch:
         is unchanged, the margin becomes a linear correlation).
         ``precision`` = "bf16x3" / "fp16x3" runs the inverse DFT stages as
         split-precision tensor-core GEMMs (``lgb_match_search_precision``);
-        "fp32" (default) is the plain FP32 search."""
+        "fp32" (default) is the plain FP32 search.
+        ``transpose`` searches the transposed micrograph (see
+        ``transposed_template_dft``): ``grid`` is then the transposed grid
+        (columns, rows), results and ``maps()`` come back in the micrograph's
+        own frame; ``transposed_template`` / ``transposed_euler`` may pass
+        precomputed ``transposed_template_dft(template_dft)`` /
+        ``transposed_euler_angles(euler_angles)`` (shared by several
+        micrographs).  Results at valid positions equal the direct search's to
+        rounding (the conjugated rotations are rounded to FP32 Euler angles)."""
         self.device = _single_cuda_device(device)
+        self.transpose = bool(transpose)
+        self.decode_euler = None
+        if self.transpose:
+            if precision != "fp32":
+                raise ValueError("a transposed search runs the plain FP32 kernels only")
+            dev0 = _single_cuda_device(device)
+            self.decode_euler = euler_angles.to(dev0, torch.float32).contiguous()
+            image_dft = transposed_image_dft(image_dft.to(dev0))
+            template_dft = (transposed_template if transposed_template is not None
+                            else transposed_template_dft(template_dft.to(dev0)))
+            ctf_filters = transposed_half_filter(ctf_filters.to(dev0))
+            whitening_filter_template = transposed_half_filter(whitening_filter_template.to(dev0))
+            euler_angles = transposed_euler if transposed_euler is not None else transposed_euler_angles(euler_angles)
         if image_dft.dim() != 2 or template_dft.dim() != 3:
             raise ValueError("image_dft must be (H, W//2+1) and template_dft (d, d, d//2+1)")
         H, wc_img = image_dft.shape
@@ -289,9 +385,11 @@ class MatchTemplateSearch:
         self.orientations_done += end - begin
 
     def maps(self) -> dict:
-        """The four running maps (device tensors, shared with the search)."""
-        return {"mip": self.mip, "best_global_index": self.best_index, "correlation_sum": self.corr_sum,
-                "correlation_squared_sum": self.corr_sq_sum}
+        """The four running maps (device tensors, shared with the search; for a
+        transposed search, transposed views in the micrograph's frame)."""
+        m = {"mip": self.mip, "best_global_index": self.best_index, "correlation_sum": self.corr_sum,
+             "correlation_squared_sum": self.corr_sq_sum}
+        return {k: v.t() for k, v in m.items()} if self.transpose else m
 
     def state_dict(self) -> dict:
         """Resumable state (CPU tensors): the four maps and the orientations
@@ -319,11 +417,12 @@ class MatchTemplateSearch:
 
     def load_maps(self, maps: dict) -> None:
         """Replace the running maps, e.g. with the reduction of every rank's maps."""
+        tr = (lambda t: t.t()) if self.transpose else (lambda t: t)
         with torch.cuda.device(self.device):
-            self.mip.copy_(maps["mip"])
-            self.best_index.copy_(maps["best_global_index"])
-            self.corr_sum.copy_(maps["correlation_sum"])
-            self.corr_sq_sum.copy_(maps["correlation_squared_sum"])
+            self.mip.copy_(tr(maps["mip"]))
+            self.best_index.copy_(tr(maps["best_global_index"]))
+            self.corr_sum.copy_(tr(maps["correlation_sum"]))
+            self.corr_sq_sum.copy_(tr(maps["correlation_squared_sum"]))
 
     def result(self, to_cpu: bool = True) -> dict:
         """Decode indices and compute mean / std / z-score (process_results.py:67-183).
@@ -349,7 +448,7 @@ class MatchTemplateSearch:
                     _ptr(self.best_index),
                     _ptr(self.corr_sum),
                     _ptr(self.corr_sq_sum),
-                    _ptr(self.euler_angles),
+                    _ptr(self.decode_euler if self.transpose else self.euler_angles),
                     _ptr(self.defocus_values),
                     _ptr(out["scaled_mip"]),
                     _ptr(out["best_phi"]),
@@ -374,6 +473,8 @@ class MatchTemplateSearch:
             }
             if (Hp, Wp) != (H, W):
                 res = {k: v[:H, :W].contiguous() for k, v in res.items()}
+            if self.transpose:
+                res = {k: v.t().contiguous() for k, v in res.items()}
             if to_cpu:
                 res = {k: v.cpu() for k, v in res.items()}
         res["total_projections"] = self.total_projections

@@ -47,8 +47,8 @@ def _search(kw, batch, **opts):
     s = MatchTemplateSearch(**kw, device=DEV, orientation_batch_size=batch, **opts)
     s.run()
     res = s.result(to_cpu=True)
-    H, W = s.shape
-    res["best_global_index"] = s.best_index[:H, :W].cpu()
+    H, W = res["mip"].shape
+    res["best_global_index"] = s.maps()["best_global_index"][:H, :W].cpu()
     res["_maps"] = {k: v.clone() for k, v in s.maps().items()}
     torch.cuda.synchronize()
     return res
@@ -188,3 +188,46 @@ def test_batched_driver_over_uneven_micrographs(tmp_path, monkeypatch):
         assert tuple(res["mip"].shape) == (H, 2 * (wc - 1))
         assert torch.equal(res["mip"], ref["mip"])
         torch.testing.assert_close(res["scaled_mip"], ref["scaled_mip"], rtol=1e-4, atol=1e-4)
+
+
+@pytest.mark.parametrize("H,W,d,grid", [(256, 512, 48, None), (288, 250, 32, None), (288, 250, 32, (256, 512))])
+def test_transposed_search_matches_oracle(H, W, d, grid):
+    """A search of the transposed micrograph with the x/y-exchanged template and
+    conjugated rotations equals the direct search (oracle) at valid positions:
+    astigmatic CTF filters, orientations at theta = 0 and 180 included,
+    compiled and zero-padded transposed grids."""
+    from leopard_em_gb300 import preprocess as pp
+
+    kw = _workload(H, W, d, 10, n_df=2, seed=9)
+    kw["euler_angles"][0] = torch.tensor([30.0, 0.0, 40.0])
+    kw["euler_angles"][1] = torch.tensor([10.0, 180.0, 70.0])
+    kw["ctf_filters"] = pp.ctf_filter_stack(d, 11000.0, 9000.0, kw["defocus_values"], kw["pixel_values"],
+                                            astigmatism_angle=30.0)
+    ref = _oracle(kw, 4)
+    gpu = _search(kw, 4, transpose=True, grid=grid)
+    assert gpu["mip"].shape == (H, W)
+    _assert_parity(gpu, ref, H - d + 1, W - d + 1)
+    for key in ("best_phi", "best_theta", "best_psi", "best_defocus"):
+        sep = ref["mip"][: H - d + 1, : W - d + 1] - ref["second_best"][: H - d + 1, : W - d + 1] > 1e-3
+        got = gpu[key][: H - d + 1, : W - d + 1]
+        want = ref[key][: H - d + 1, : W - d + 1].to(got.dtype)
+        assert bool((got[sep] == want[sep]).all()), key
+
+
+def test_autotuner_may_pick_a_transposed_grid_and_keeps_results():
+    """The tuner times both orientations of a non-square micrograph; whichever
+    it picks, the batched driver's maps agree with the oracle."""
+    kw = _workload(288, 128, 32, 8, seed=11)
+    t = autotune.tune_search(kw["image_dft"], kw["template_dft"], kw["ctf_filters"], kw["whitening_filter_template"],
+                             kw["defocus_values"], kw["pixel_values"], kw["euler_angles"], DEV, n_probe=8,
+                             use_cache=False)
+    assert isinstance(t.transpose, bool)
+    mic = {k: kw[k] for k in ("image_dft", "ctf_filters", "whitening_filter_template", "defocus_values",
+                               "pixel_values")}
+    res, rep = match_template_batch([mic], kw["template_dft"], kw["euler_angles"], DEV, tune=True, tune_cache=False)
+    ref = _oracle(kw, 4)
+    r = res[0]
+    sl = (slice(0, 288 - 32 + 1), slice(0, 128 - 32 + 1))
+    scale = ref["mip"][sl].double().abs().clamp_min(1.0)
+    assert ((r["mip"][sl].double() - ref["mip"][sl].double()).abs() / scale).max().item() <= MIP_RTOL
+    assert (r["scaled_mip"][sl].double() - ref["scaled_mip"][sl].double()).abs().max().item() <= Z_ATOL
