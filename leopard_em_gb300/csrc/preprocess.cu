@@ -7,8 +7,10 @@
 // pydantic_models/config/correlation_filters.py:16-410 (whitening and
 // bandpass filters through torch-fourier-filter), utils/image_processing.py:
 // 16-75 (preprocess_image).  Frequencies are those of torch.fft.fftfreq /
-// rfftfreq (cycles per pixel), computed in FP64 without contraction so that
-// bin assignment matches a host FP64 evaluation of the same formula.
+// rfftfreq and numpy.fft.fftfreq (cycles per pixel): index times the FP64
+// reciprocal of the length, squared and summed without contraction, so that
+// the nearest-bin assignment of |k| -- which has exact ties, e.g. |k| = 97.5
+// bins on a 256 x 288 grid -- rounds the way a host evaluation does.
 #include <math.h>
 
 #include "common.cuh"
@@ -16,11 +18,11 @@
 namespace lgb {
 
 __device__ __forceinline__ double fftfreq_d(int i, int n) {
-  return __ddiv_rn((double)(i < (n + 1) / 2 ? i : i - n), (double)n);
+  return __dmul_rn((double)(i < (n + 1) / 2 ? i : i - n), __ddiv_rn(1.0, (double)n));
 }
 // |k| of rfft bin (y, x) of an h x w real grid, cycles per pixel
 __device__ __forceinline__ double rfft_radius(int y, int x, int h, int w) {
-  const double ky = fftfreq_d(y, h), kx = __ddiv_rn((double)x, (double)w);
+  const double ky = fftfreq_d(y, h), kx = __dmul_rn((double)x, __ddiv_rn(1.0, (double)w));
   return sqrt(__dadd_rn(__dmul_rn(kx, kx), __dmul_rn(ky, ky)));
 }
 __device__ __forceinline__ int radial_bin(double r, double fmax, int nb) {
@@ -46,7 +48,7 @@ __global__ void ctf_stack_kernel(int d, double du, double dv, double ang_deg, co
     const int cs = (int)(e / (plane * D));
     const int y = xy / wc, x = xy % wc;
     const double ky = fftfreq_d(y, d) / prm.pixel_size;
-    const double kx = (double)x / d / prm.pixel_size;
+    const double kx = fftfreq_d(x, d) / prm.pixel_size;
     const double k2 = kx * kx + ky * ky;
     const double ang = atan2(ky, kx);
     const double defocus = (double)dfo[df] + 0.5 * (du + dv);

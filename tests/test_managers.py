@@ -273,9 +273,12 @@ def test_refine_manager_from_yaml_recovers_planted_poses(tmp_path):
     assert eul.shape == (2, 3)
     z = torch.as_tensor(res["refined_z_score"]).reshape(-1)
     assert bool((z > 5.0).all()), z
-    # the planted poses lie inside the local grid: the best offset is the null offset
-    planted = torch.tensor([p[3] for p in wl.planted], dtype=torch.float32)
-    d = (eul.float() - planted).abs()
-    d = torch.minimum(d, 360.0 - d)
-    assert float(d.max()) <= 1.01, (eul, planted)
+    # the planted poses lie inside the local grid (+-2 deg): the refined
+    # rotation is within a grid step or two of the planted one
+    from leopard_em_gb300.proposal import angular_error_deg
+    from leopard_em_gb300.rotations import euler_zyz_to_rotmat
+
+    planted = torch.tensor([p[3] for p in wl.planted], dtype=torch.float64)
+    err = angular_error_deg(euler_zyz_to_rotmat(eul.double()), euler_zyz_to_rotmat(planted))
+    assert float(err.max()) <= 2.5, (eul, planted, err)
     assert np.allclose(np.asarray(res["refined_pos_y"]).reshape(-1), 0.0, atol=1.0)

@@ -192,9 +192,17 @@ def test_production_configuration_against_oracle():
     """The production configuration's own inputs -- 4096^2 micrograph with 300
     projections planted at SNR 0.1, the 4000-blob 384^3 template at 1.06 A/px,
     3 defocus planes (-200/0/+200 A) -- over 24 consecutive orientations of its
-    2.5/1.5-degree grid (3 batches of 8, as configured), against the oracle
-    (FP32 correlograms, FP64 statistics, runner-up tracked per pixel).  The
-    oracle runs its torch operations on the GPU (cuFFT) to finish in seconds."""
+    2.5/1.5-degree grid (3 batches of 8, as configured).
+
+    At this size the FP32 restatement of the reference drifts from the exact
+    result: it builds rotation matrices in FP32 from FP32 Euler angles (as the
+    reference's roma call does), and a 1e-7 rotation error over a 384-voxel
+    template moves correlogram values by ~1e-3 relative (measured 2.0e-3 on the
+    MIP against the FP64 oracle).  The CUDA path builds rotations in FP64, so
+    parity is asserted against the FP64 oracle (FP64 correlograms and
+    statistics, runner-up tracked), and the CUDA path must be closer to it than
+    the FP32 restatement is.  Both oracles run their torch operations on the GPU
+    (cuFFT) to finish in seconds."""
     cfg = sy.CONFIG_PRODUCTION
     wl = sy.make_match_workload(cfg, device="cuda:0")
     kw = dict(wl.kwargs)
@@ -203,6 +211,15 @@ def test_production_configuration_against_oracle():
     assert kw["ctf_filters"].shape[:2] == (1, 3) and kw["template_dft"].shape == (384, 384, 193)
     gpu = _gpu_search(kw, cfg.orientation_batch)
     ref = orc.core_match_template_cpu(**kw, orientation_batch_size=cfg.orientation_batch, backend="batched",
-                                      stat_dtype=torch.float64, track_second_best=True, device="cuda:0")
+                                      stat_dtype=torch.float64, compute_dtype=torch.float64,
+                                      track_second_best=True, device="cuda:0")
     torch.cuda.empty_cache()
     _assert_parity(gpu, ref, second=ref["second_best"])
+    f32 = orc.core_match_template_cpu(**kw, orientation_batch_size=cfg.orientation_batch, backend="batched",
+                                      stat_dtype=torch.float64, device="cuda:0")
+    torch.cuda.empty_cache()
+    scale = ref["mip"].double().abs().clamp_min(1.0)
+    err_gpu = ((gpu["mip"].double() - ref["mip"].double()).abs() / scale).max().item()
+    err_f32 = ((f32["mip"].double() - ref["mip"].double()).abs() / scale).max().item()
+    print(f"MIP relative error vs FP64: CUDA path {err_gpu:.2e}, FP32 restatement {err_f32:.2e}")
+    assert err_gpu < err_f32

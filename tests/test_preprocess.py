@@ -73,7 +73,7 @@ def test_device_kernels_match_oracle():
     dev = torch.device("cuda:0")
     ctf = _ctf_package(dev)
     assert ctf.is_cuda and np.abs(ctf.cpu().numpy() - GOLD["ctf/out"]).max() < 2e-5
-    for h, w in ((96, 128), (4096, 4096)):
+    for h, w in ((96, 128), (256, 288), (4096, 4096)):  # 256 x 288 has exact nearest-bin ties
         img = _image(h, w, 4)
         for out_shape, nb, fmax, power in (((32, 32), None, 0.5, True), ((h, w), 40, 0.4, False),
                                            ((384, 384), None, 0.5, True)):
