@@ -34,6 +34,7 @@ from ._native import lib
 CACHE_ENV = "LEOPARD_EM_GB300_TUNE_CACHE"
 DEFAULT_BATCHES = (2, 4, 8, 12, 16)
 DEFAULT_WAVES = (2, 4, 8)
+TRANSPOSE_GAIN = 0.9  # a transposed grid must time at most this fraction of the best direct one
 _lock = threading.Lock()
 
 
@@ -176,7 +177,15 @@ def tune_search(image_dft, template_dft, ctf_filters, whitening_filter_template,
         w0 = 4 if 4 in waves else waves[0]
         b0 = 8 if 8 in batches else batches[0]
         grid_cands = [g for g in grids if fits(g, b0)] or grids[:1]
-        best_g = min(grid_cands, key=lambda g: time_of((g, b0, w0)))
+        direct = [g for g in grid_cands if not g[1]] or grid_cands[:1]
+        best_g = min(direct, key=lambda g: time_of((g, b0, w0)))
+        # a transposed search also pays a transposed spectrum per micrograph:
+        # take it only when its orientations run clearly faster
+        trans = [g for g in grid_cands if g[1]]
+        if trans:
+            best_t = min(trans, key=lambda g: time_of((g, b0, w0)))
+            if time_of((best_t, b0, w0)) < TRANSPOSE_GAIN * time_of((best_g, b0, w0)):
+                best_g = best_t
         cands = [b for b in batches if b >= 1 and fits(best_g, b)] or [1]
         best_b = min(cands, key=lambda b: time_of((best_g, b, w0)))
         best_w = min(waves, key=lambda w: time_of((best_g, best_b, w)))

@@ -48,7 +48,7 @@ __global__ void ctf_stack_kernel(int d, double du, double dv, double ang_deg, co
     const int cs = (int)(e / (plane * D));
     const int y = xy / wc, x = xy % wc;
     const double ky = fftfreq_d(y, d) / prm.pixel_size;
-    const double kx = fftfreq_d(x, d) / prm.pixel_size;
+    const double kx = __dmul_rn((double)x, __ddiv_rn(1.0, (double)d)) / prm.pixel_size;  // rfftfreq: x >= 0
     const double k2 = kx * kx + ky * ky;
     const double ang = atan2(ky, kx);
     const double defocus = (double)dfo[df] + 0.5 * (du + dv);

@@ -178,10 +178,12 @@ def test_batched_driver_over_uneven_micrographs(tmp_path, monkeypatch):
     results, report = match_template_batch(mics, template[0], eul, DEV, orientation_range=(0, 16))
     assert len(results) == 4 and len(report.ms) == 4 and all(ms > 0 for ms in report.ms)
     assert report.percentile(50) <= report.percentile(99)
-    for m, res, grid in zip(mics, results, report.grids):
-        # same grid as the driver chose (the tuner may pad past the smallest one)
+    for m, res, grid, tun in zip(mics, results, report.grids, report.tunings):
+        # same grid and orientation as the driver chose (the tuner may pad past
+        # the smallest grid, or search the transposed micrograph)
         single = MatchTemplateSearch(**m, template_dft=template[0], euler_angles=eul, device=DEV,
-                                     orientation_batch_size=4, grid=grid)
+                                     orientation_batch_size=tun.orientation_batch, grid=grid,
+                                     transpose=tun.transpose)
         single.run(0, 16)
         ref = single.result(to_cpu=True)
         H, wc = m["image_dft"].shape
