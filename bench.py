@@ -61,7 +61,9 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--config", choices=["production", "small", "refbench"], default="production",
                     help="refbench: the reference's published benchmark shape (4096^2, 512^3, 11 defocus)")
-    ap.add_argument("--batch", type=int, default=0, help="orientation batch (0: the configuration's)")
+    ap.add_argument("--batch", type=int, default=-1,
+                    help="orientation batch (0: the configuration's; -1: 16 for the production and reference-"
+                         "benchmark shapes, which the autotuner picks for a 4096^2 grid, else the configuration's)")
     ap.add_argument("--refine-particles", type=int, default=128)
     ap.add_argument("--no-refine", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
@@ -690,7 +692,9 @@ def main():
     cfg = wl.config
     kw = wl.kwargs
     N = kw["euler_angles"].shape[0]
-    B = args.batch or cfg.orientation_batch
+    B = args.batch if args.batch > 0 else cfg.orientation_batch
+    if args.batch < 0 and args.config in ("production", "refbench"):
+        B = 16
     chunk = max(B, (args.orient_per_step // B) * B)
     search = MatchTemplateSearch(**kw, device=dev, orientation_batch_size=B)
     stream = torch.cuda.current_stream(dev)

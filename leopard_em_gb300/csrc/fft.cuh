@@ -249,6 +249,14 @@ struct IdxPad16 {
   static __device__ __forceinline__ int f(int i) { return i + (i >> 4); }
 };
 
+// two float2 of padding per 16 elements: the layout between the two radix-8
+// middle passes of a 2048-point transform, where the stride-8 stores of the
+// first and the stride-256 loads of the second are both conflict free
+struct IdxPad16x2 {
+  __host__ __device__ static constexpr int pad(int n) { return n + 2 * (n / 16); }
+  static __device__ __forceinline__ int f(int i) { return i + 2 * (i >> 4); }
+};
+
 // One Stockham pass.  NZ >= 0 marks a pruned first pass whose inputs at index
 // >= nz are known zeros (nz given at run time); they are not read.
 template <int N, int R, int NS, int NT, int DIR, class IDX, bool PRUNED>
@@ -446,6 +454,8 @@ template <class IDX, int STEP>
 __device__ __forceinline__ int padded_at(int fbase, int base, int q) {
   if constexpr (std::is_same<IDX, IdxPad16>::value && STEP % 16 == 0) {
     return fbase + q * (STEP + STEP / 16);
+  } else if constexpr (std::is_same<IDX, IdxPad16x2>::value && STEP % 16 == 0) {
+    return fbase + q * (STEP + 2 * (STEP / 16));
   } else {
     return IDX::f(base + q * STEP);
   }
@@ -510,6 +520,38 @@ __device__ __forceinline__ void table_pass(float2* __restrict__ x, const float2*
       const int fb = IDX::f(base);
 #pragma unroll
       for (int q = 0; q < R; ++q) x[padded_at<IDX, NS>(fb, base, q)] = v[p][q];
+    }
+  }
+  __syncthreads();
+}
+
+// The same pass reading with one index map and writing with another (the
+// buffer then changes layout between passes).
+template <int N, int R, int NS, int NT, int DIR, class IDX_LD, class IDX_ST>
+__device__ __forceinline__ void table_pass_io(float2* __restrict__ x, const float2* __restrict__ tab, int t) {
+  constexpr int NB = N / R;
+  constexpr int PER = (NB + NT - 1) / NT;
+  float2 v[PER][R];
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int j = t + p * NT;
+    if ((NB % NT == 0) || j < NB) {
+      const int fj = IDX_LD::f(j);
+#pragma unroll
+      for (int q = 0; q < R; ++q) v[p][q] = x[padded_at<IDX_LD, NB>(fj, j, q)];
+      if (NS > 1) twiddle_from_table<R, DIR, NS>(v[p], tab, j % NS);
+      Dft<R, DIR>::run(v[p]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int j = t + p * NT;
+    if ((NB % NT == 0) || j < NB) {
+      const int base = (j / NS) * NS * R + (j % NS);
+      const int fb = IDX_ST::f(base);
+#pragma unroll
+      for (int q = 0; q < R; ++q) x[padded_at<IDX_ST, NS>(fb, base, q)] = v[p][q];
     }
   }
   __syncthreads();

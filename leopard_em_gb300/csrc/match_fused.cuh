@@ -405,7 +405,9 @@ struct RowFused {
   static constexpr int PER1 = (NB1 + NT - 1) / NT;
   static constexpr int NBL = WH / RLAST;
   static constexpr int PERL = NBL / NT;
-  static constexpr int ZS = IdxPad16::pad(WH) + 2;
+  // the 8, 8 middle passes of 2048 = 8 8 8 4 store / load through the 16x2 layout
+  static constexpr bool MID88 = std::is_same<typename Middle<RL>::type, Radices<8, 8>>::value;
+  static constexpr int ZS = (MID88 ? IdxPad16x2::pad(WH) : IdxPad16::pad(WH)) + 2;
   static constexpr int TAB = TableSize<1, RL>::value;
   static_assert(NBL % NT == 0, "last pass must give every thread whole butterflies");
   static_assert(NB1 <= NT * PER1, "first pass coverage");
@@ -506,7 +508,14 @@ __global__ void __launch_bounds__(NT, 3)
       }
     }
     __syncthreads();
-    TablePasses<WH, NT, +1, IdxPad16, R1, typename Middle<RL>::type>::run(z, tab, t);
+    if constexpr (RF::MID88) {
+      // stride-8 radix-8 stores into the 16x2 layout, read back by the
+      // stride-64 pass, which stores the plain padded layout again
+      table_pass_io<WH, 8, R1, NT, +1, IdxPad16, IdxPad16x2>(z, tab, t);
+      table_pass_io<WH, 8, R1 * 8, NT, +1, IdxPad16x2, IdxPad16>(z, tab + R1 * 7, t);
+    } else {
+      TablePasses<WH, NT, +1, IdxPad16, R1, typename Middle<RL>::type>::run(z, tab, t);
+    }
     // ---- last pass -> registers -> statistics
 #pragma unroll
     for (int p = 0; p < PERL; ++p) {
