@@ -77,6 +77,8 @@ def _args():
     ap.add_argument("--precision-error-orient", type=int, default=10240,
                     help="orientations (uniform random) checked against the FP64 oracle on the small configuration")
     ap.add_argument("--batched-micrographs", type=int, default=12)
+    ap.add_argument("--batched-full-grid", type=int, default=-1,
+                    help="only time one batched-workload micrograph (this index) over its full grid")
     ap.add_argument("--batched-orient", type=int, default=48,
                     help="orientations searched per micrograph in the batched-form sample")
     return ap.parse_args()
@@ -510,6 +512,34 @@ def batched_bench(args, dev):
     }
 
 
+def batched_full_grid(args):
+    """One micrograph of the batched workload (``--batched-full-grid I``: its
+    index, 0 = the 2048^2 one) searched over the whole 3.0/2.0-degree grid
+    (825,480 orientations x 7 defocus x 3 pixel sizes) through the batched
+    driver, autotuned and graph-replayed; device time from the upload of its
+    spectrum to its finalised maps.  Not part of the default run (minutes)."""
+    from leopard_em_gb300 import synthetic as sy
+    from leopard_em_gb300.backend.batched import match_template_batch
+
+    dev = torch.device("cuda", 0)
+    i = int(args.batched_full_grid)
+    template_dft, eul, mics, cfgs = sy.make_batched_workload(i + 1, device=dev)
+    n_cd = len(sy.CONFIG_BATCHED.defocus_offsets) * len(sy.CONFIG_BATCHED.pixel_size_offsets)
+    mic = [mics[i]]
+    match_template_batch(mic, template_dft, eul, dev, orientation_range=(0, 64), tune=True)  # tune + warm up
+    torch.cuda.synchronize(dev)
+    with ClockSampler(0) as clocks:
+        t0 = time.perf_counter()
+        res, rep = match_template_batch(mic, template_dft, eul, dev, tune=True)
+        wall = time.perf_counter() - t0
+    N = int(eul.shape[0])
+    return {"metric": "full-grid search time of one micrograph (batched form)", "value": rep.ms[0] / 1e3,
+            "unit": "s", "micrograph": list(cfgs[i].image_shape), "orientations": N, "defocus_x_pixel_sizes": n_cd,
+            "cross_correlations": N * n_cd, "cross_correlations_per_s": N * n_cd / (rep.ms[0] / 1e3),
+            "wall_s": wall, "grid": list(rep.grids[0]), "tuning": rep.tunings[0].__dict__,
+            "clocks": clocks.summary()}
+
+
 def refine_plain_only(args):
     """Plain refinement grid alone (device-timed particles/s), for profiling."""
     from leopard_em_gb300 import synthetic as sy
@@ -596,6 +626,52 @@ def refine_bench(args, dev, with_cpu):
     return out
 
 
+def network_timing(dev, infer_batch=1024, train_batch=256, reps=5):
+    """Proposal-network time per particle through the tensor-core kernels:
+    inference (forward at ``infer_batch``) and one training step (forward,
+    backward, Adam at ``train_batch``), CUDA events on the current stream."""
+    from leopard_em_gb300 import proposal as pr
+
+    net = pr.ProposalNet(dev, seed=0)
+    g = torch.Generator().manual_seed(5)
+    x = torch.randn(infer_batch, pr.CHANNELS, pr.BAND, pr.BAND, generator=g).to(dev, torch.bfloat16)
+    tgt = torch.randn(train_batch, 7, generator=g).to(dev)
+    flops = 0  # multiply-adds x 2 per sample, forward
+    hw = pr.BAND
+    for kind, cin, cout, stride, _ in pr.LAYERS:
+        if kind == "conv":
+            hw = (hw - 1) // stride + 1
+            flops += 2 * hw * hw * cout * cin * 9
+        else:
+            flops += 2 * cin * cout
+
+    def train_step():
+        out = net.forward(x[:train_batch])
+        _, dout = net.loss_and_grad(out, tgt)
+        net.backward(dout)
+        net.adam_step(1e-4)
+
+    res = {}
+    for label, fn, n in (("inference", lambda: net.forward(x), infer_batch), ("train_step", train_step, train_batch)):
+        for _ in range(3):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        sec = e0.elapsed_time(e1) / 1e3 / reps
+        mult = 1 if label == "inference" else 3  # backward ~ 2x forward
+        res[label] = {"us_per_particle": 1e6 * sec / n, "batch": n, "ms_per_batch": 1e3 * sec,
+                      "tflops": mult * flops * n / sec / 1e12}
+    net.check_device_status()
+    res["forward_mflop_per_particle"] = flops / 1e6
+    res["kernels"] = "conv3x3 (implicit GEMM) and linear layers on tcgen05: BF16 operands, FP32 TMEM accumulation"
+    return res
+
+
 def learned_refine_bench(kw, dev, cfg, plain_res, n_plain):
     """Learned proposals + small local grid (fallback: full plain grid) on the
     same particles as the plain grid, and the Gauss-Newton-only ablation (the
@@ -636,6 +712,7 @@ def learned_refine_bench(kw, dev, cfg, plain_res, n_plain):
                       "small_grid": "+-0.5 deg @ 0.125 x +-100 A @ 50",
                       "timing": "wall clock, host tensors in and out (network inputs, inference, two refinement "
                                 "calls and any fallback)"}
+    out["network_timing"] = network_timing(dev)
     return out
 
 
@@ -678,6 +755,9 @@ def main():
         return
     if args.refine_plain_only:
         print(json.dumps(refine_plain_only(args)), flush=True)
+        return
+    if args.batched_full_grid >= 0:
+        print(json.dumps(batched_full_grid(args)), flush=True)
         return
     rank, world, local = _dist()
     if world > 1 and not torch.distributed.is_initialized():

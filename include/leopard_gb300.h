@@ -395,17 +395,33 @@ int lgb_preprocess_image(int n_images, int image_h, int image_w, const void* ima
 /* gradients FP32.  NCHW; conv weights [Cout][Cin][3][3]; linear [Out][In]. */
 /* ------------------------------------------------------------------------ */
 
-/* y = act(conv3x3(x, w, pad 1, stride 1|2) + b); act = ReLU if relu. */
+/* 3x3 convolutions (pad 1, stride 1|2, 1 <= Cin, Cout <= 128) as implicit
+ * GEMMs on the tcgen05 tensor cores: BF16 operands, FP32 accumulation.
+ * workspace (device, 256-byte aligned) holds the gathered operands; its size
+ * for one layer shape (forward or backward) comes from
+ * lgb_nn_conv3x3_workspace_size.  device_status (device int, caller-zeroed)
+ * receives LGB_ERR_DEVICE_TIMEOUT if a bounded device wait ran out. */
+int lgb_nn_conv3x3_workspace_size(int N, int Cin, int H, int W, int Cout, int stride, size_t* bytes);
+/* y = act(conv3x3(x, w) + b) in BF16; act = ReLU if relu; b optional. */
 int lgb_nn_conv3x3_forward(int N, int Cin, int H, int W, int Cout, int stride, int relu, const void* x,
-                           const void* w, const float* b, void* y, void* stream);
+                           const void* w, const float* b, void* y, void* workspace, size_t workspace_bytes,
+                           int* device_status, void* stream);
 /* From g = dLoss/d(pre-activation output): dx (optional), dw, db (optional). */
 int lgb_nn_conv3x3_backward(int N, int Cin, int H, int W, int Cout, int stride, const void* x, const void* w,
-                            const float* g, float* dx, float* dw, float* db, void* stream);
-/* y[n][o] = act(sum_i x[n][i] w[o][i] + b[o]) into y_bf16 and/or y_f32. */
+                            const float* g, float* dx, float* dw, float* db, void* workspace, size_t workspace_bytes,
+                            int* device_status, void* stream);
+/* Linear layers on the tcgen05 tensor cores (BF16 operands, FP32
+ * accumulation), with the same workspace and device_status contract as the
+ * convolutions; lgb_nn_linear_workspace_size covers forward and backward.
+ * y[n][o] = act(sum_i x[n][i] w[o][i] + b[o]) into y_bf16 and/or y_f32. */
+int lgb_nn_linear_workspace_size(int N, int In, int Out, size_t* bytes);
 int lgb_nn_linear_forward(int N, int In, int Out, int relu, const void* x, const void* w, const float* b,
-                          void* y_bf16, float* y_f32, void* stream);
+                          void* y_bf16, float* y_f32, void* workspace, size_t workspace_bytes, int* device_status,
+                          void* stream);
+/* From g = dLoss/dy (pre-activation): dx (optional), dw, db (optional). */
 int lgb_nn_linear_backward(int N, int In, int Out, const void* x, const void* w, const float* g, float* dx,
-                           float* dw, float* db, void* stream);
+                           float* dw, float* db, void* workspace, size_t workspace_bytes, int* device_status,
+                           void* stream);
 /* g = dy * (y > 0) for a ReLU output y (bf16). */
 int lgb_nn_relu_backward(long long n, const void* y, const float* dy, float* g, void* stream);
 /* loss = mean_n sum_d w_d (pred - target)^2 and its gradient (weights optional). */

@@ -117,10 +117,12 @@ _SIGNATURES = {
     "lgb_bandpass_filter": ([_I, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double, _P, _P], _I),
     "lgb_preprocess_image": ([_I, _I, _I, _P, _P, _LL, _P, ctypes.c_double, _P, _P, _P], _I),
     "lgb_tc_gemm": ([_I] * 6 + [_P] * 5 + [_I, _I, _I, _P, _P], _I),
-    "lgb_nn_conv3x3_forward": ([_I] * 7 + [_P] * 4 + [_P], _I),
-    "lgb_nn_conv3x3_backward": ([_I] * 6 + [_P] * 6 + [_P], _I),
-    "lgb_nn_linear_forward": ([_I] * 4 + [_P] * 5 + [_P], _I),
-    "lgb_nn_linear_backward": ([_I] * 3 + [_P] * 6 + [_P], _I),
+    "lgb_nn_conv3x3_workspace_size": ([_I] * 6 + [ctypes.POINTER(_SZ)], _I),
+    "lgb_nn_conv3x3_forward": ([_I] * 7 + [_P] * 5 + [_SZ, _P, _P], _I),
+    "lgb_nn_conv3x3_backward": ([_I] * 6 + [_P] * 7 + [_SZ, _P, _P], _I),
+    "lgb_nn_linear_workspace_size": ([_I] * 3 + [ctypes.POINTER(_SZ)], _I),
+    "lgb_nn_linear_forward": ([_I] * 4 + [_P] * 6 + [_SZ, _P, _P], _I),
+    "lgb_nn_linear_backward": ([_I] * 3 + [_P] * 7 + [_SZ, _P, _P], _I),
     "lgb_nn_relu_backward": ([_LL, _P, _P, _P, _P], _I),
     "lgb_nn_mse": ([_I, _I] + [_P] * 5 + [_P], _I),
     "lgb_nn_adam": ([_LL] + [_P] * 5 + [ctypes.c_float] * 5 + [_I, _P], _I),

@@ -4,7 +4,9 @@
 //
 // Storage: activations and forward weights BF16; accumulation FP32; gradients,
 // master weights and Adam moments FP32.  Layout NCHW; conv weights
-// [Cout][Cin][3][3]; linear weights [Out][In].
+// [Cout][Cin][3][3]; linear weights [Out][In].  The convolutions and linear
+// layers run on the tensor cores (nn_tc.cu); this file holds the ReLU
+// gradient, the loss, Adam and the input builder.
 //
 // Also: the network's input builder (lgb_nn_make_inputs): a low-frequency band
 // of each particle spectrum and the template's central slice at the particle's
@@ -19,180 +21,6 @@ namespace lgb {
 
 using bf16 = __nv_bfloat16;
 
-__device__ __forceinline__ float ldf(const bf16* p) { return __bfloat162float(*p); }
-__device__ __forceinline__ float ldf(const float* p) { return *p; }
-
-// ---- 3x3 convolution, pad 1, stride s ------------------------------------
-__global__ void conv3x3_fwd_kernel(int N, int Cin, int H, int W, int Cout, int s, int relu, const bf16* __restrict__ x,
-                                   const bf16* __restrict__ w, const float* __restrict__ b, bf16* __restrict__ y) {
-  const int Ho = (H - 1) / s + 1, Wo = (W - 1) / s + 1;
-  const long long n_out = (long long)N * Cout * Ho * Wo;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_out;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int ox = (int)(i % Wo);
-    const int oy = (int)((i / Wo) % Ho);
-    const int co = (int)((i / ((long long)Wo * Ho)) % Cout);
-    const int n = (int)(i / ((long long)Wo * Ho * Cout));
-    float acc = b ? b[co] : 0.f;
-    const bf16* wr = w + (size_t)co * Cin * 9;
-    for (int ci = 0; ci < Cin; ++ci) {
-      const bf16* xc = x + ((size_t)n * Cin + ci) * H * W;
-#pragma unroll
-      for (int ky = 0; ky < 3; ++ky) {
-        const int iy = oy * s - 1 + ky;
-        if (iy < 0 || iy >= H) continue;
-#pragma unroll
-        for (int kx = 0; kx < 3; ++kx) {
-          const int ix = ox * s - 1 + kx;
-          if (ix < 0 || ix >= W) continue;
-          acc = fmaf(ldf(xc + iy * W + ix), ldf(wr + ci * 9 + ky * 3 + kx), acc);
-        }
-      }
-    }
-    if (relu && acc < 0.f) acc = 0.f;
-    y[i] = __float2bfloat16(acc);
-  }
-}
-
-// g: gradient w.r.t. the (pre-activation) output, f32 [N][Cout][Ho][Wo]
-__global__ void conv3x3_bwd_data_kernel(int N, int Cin, int H, int W, int Cout, int s, const float* __restrict__ g,
-                                        const bf16* __restrict__ w, float* __restrict__ dx) {
-  const int Ho = (H - 1) / s + 1, Wo = (W - 1) / s + 1;
-  const long long n_in = (long long)N * Cin * H * W;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_in;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int ix = (int)(i % W);
-    const int iy = (int)((i / W) % H);
-    const int ci = (int)((i / ((long long)W * H)) % Cin);
-    const int n = (int)(i / ((long long)W * H * Cin));
-    float acc = 0.f;
-    for (int co = 0; co < Cout; ++co) {
-      const float* gc = g + ((size_t)n * Cout + co) * Ho * Wo;
-      const bf16* wr = w + ((size_t)co * Cin + ci) * 9;
-#pragma unroll
-      for (int ky = 0; ky < 3; ++ky) {
-        const int t = iy + 1 - ky;
-        if (t < 0 || t % s) continue;
-        const int oy = t / s;
-        if (oy >= Ho) continue;
-#pragma unroll
-        for (int kx = 0; kx < 3; ++kx) {
-          const int u = ix + 1 - kx;
-          if (u < 0 || u % s) continue;
-          const int ox = u / s;
-          if (ox >= Wo) continue;
-          acc = fmaf(gc[oy * Wo + ox], ldf(wr + ky * 3 + kx), acc);
-        }
-      }
-    }
-    dx[i] = acc;
-  }
-}
-
-// dw[co][ci][k] = sum over n, oy, ox; one CTA of 256 threads per (co, ci); db per co (ci == 0 CTA)
-__global__ void conv3x3_bwd_weight_kernel(int N, int Cin, int H, int W, int Cout, int s, const float* __restrict__ g,
-                                          const bf16* __restrict__ x, float* __restrict__ dw, float* __restrict__ db) {
-  const int Ho = (H - 1) / s + 1, Wo = (W - 1) / s + 1;
-  const int co = blockIdx.x / Cin, ci = blockIdx.x % Cin;
-  float acc[10];
-#pragma unroll
-  for (int k = 0; k < 10; ++k) acc[k] = 0.f;
-  const long long n_pos = (long long)N * Ho * Wo;
-  for (long long i = threadIdx.x; i < n_pos; i += blockDim.x) {
-    const int ox = (int)(i % Wo);
-    const int oy = (int)((i / Wo) % Ho);
-    const int n = (int)(i / ((long long)Wo * Ho));
-    const float gv = g[((size_t)n * Cout + co) * Ho * Wo + oy * Wo + ox];
-    acc[9] += gv;
-    const bf16* xc = x + ((size_t)n * Cin + ci) * H * W;
-#pragma unroll
-    for (int ky = 0; ky < 3; ++ky) {
-      const int iy = oy * s - 1 + ky;
-      if (iy < 0 || iy >= H) continue;
-#pragma unroll
-      for (int kx = 0; kx < 3; ++kx) {
-        const int ix = ox * s - 1 + kx;
-        if (ix < 0 || ix >= W) continue;
-        acc[ky * 3 + kx] = fmaf(gv, ldf(xc + iy * W + ix), acc[ky * 3 + kx]);
-      }
-    }
-  }
-  __shared__ float red[10][8];
-#pragma unroll
-  for (int k = 0; k < 10; ++k) {
-    float v = acc[k];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < 10) {
-    float v = 0.f;
-    for (int w8 = 0; w8 < (int)(blockDim.x >> 5); ++w8) v += red[threadIdx.x][w8];
-    if (threadIdx.x < 9)
-      dw[((size_t)co * Cin + ci) * 9 + threadIdx.x] = v;
-    else if (ci == 0 && db)
-      db[co] = v;
-  }
-}
-
-// ---- generic tiled SIMT GEMM with strides: C[m][n] = sum_k A(m,k) B(k,n) (+bias, relu) ----
-template <class TA, class TB>
-__global__ void __launch_bounds__(256)
-    gemm_kernel(int M, int N, int K, const TA* __restrict__ A, long long sam, long long sak, const TB* __restrict__ B,
-                long long sbk, long long sbn, float* __restrict__ C, const float* __restrict__ bias_n, int relu,
-                bf16* __restrict__ Cbf) {
-  __shared__ float As[16][64 + 1];
-  __shared__ float Bs[16][64 + 1];
-  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
-  float acc[4][4] = {};
-  for (int k0 = 0; k0 < K; k0 += 16) {
-    for (int e = threadIdx.x; e < 16 * 64; e += 256) {
-      const int kk = e / 64, mm = e % 64;
-      const int m = m0 + mm, k = k0 + kk;
-      As[kk][mm] = (m < M && k < K) ? ldf(A + m * sam + k * sak) : 0.f;
-      const int n = n0 + mm;
-      Bs[kk][mm] = (n < N && k < K) ? ldf(B + k * sbk + n * sbn) : 0.f;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < 16; ++kk) {
-      float a[4], bb[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) bb[j] = Bs[kk][tx * 4 + j];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], bb[j], acc[i][j]);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int m = m0 + ty * 4 + i;
-    if (m >= M) continue;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int n = n0 + tx * 4 + j;
-      if (n >= N) continue;
-      float v = acc[i][j] + (bias_n ? bias_n[n] : 0.f);
-      if (relu && v < 0.f) v = 0.f;
-      if (C) C[(size_t)m * N + n] = v;
-      if (Cbf) Cbf[(size_t)m * N + n] = __float2bfloat16(v);
-    }
-  }
-}
-
-__global__ void colsum_kernel(int M, int N, const float* __restrict__ g, float* __restrict__ out) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= N) return;
-  float s = 0.f;
-  for (int m = 0; m < M; ++m) s += g[(size_t)m * N + n];
-  out[n] = s;
-}
 
 __global__ void relu_bwd_kernel(long long n, const bf16* __restrict__ y, const float* __restrict__ dy,
                                 float* __restrict__ g) {
@@ -607,58 +435,6 @@ static int g256(long long n) {
 using namespace lgb;
 
 extern "C" {
-
-int lgb_nn_conv3x3_forward(int N, int Cin, int H, int W, int Cout, int stride, int relu, const void* x, const void* w,
-                           const float* b, void* y, void* stream) {
-  if (N < 1 || Cin < 1 || H < 1 || W < 1 || Cout < 1 || (stride != 1 && stride != 2) || !x || !w || !y)
-    return LGB_ERR_INVALID_ARGUMENT;
-  const long long n = (long long)N * Cout * ((H - 1) / stride + 1) * ((W - 1) / stride + 1);
-  conv3x3_fwd_kernel<<<g256(n), 256, 0, (cudaStream_t)stream>>>(N, Cin, H, W, Cout, stride, relu,
-                                                                 static_cast<const bf16*>(x),
-                                                                 static_cast<const bf16*>(w), b, static_cast<bf16*>(y));
-  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
-}
-
-int lgb_nn_conv3x3_backward(int N, int Cin, int H, int W, int Cout, int stride, const void* x, const void* w,
-                            const float* g, float* dx, float* dw, float* db, void* stream) {
-  if (N < 1 || Cin < 1 || H < 1 || W < 1 || Cout < 1 || (stride != 1 && stride != 2) || !x || !w || !g || !dw)
-    return LGB_ERR_INVALID_ARGUMENT;
-  cudaStream_t s = (cudaStream_t)stream;
-  if (dx)
-    conv3x3_bwd_data_kernel<<<g256((long long)N * Cin * H * W), 256, 0, s>>>(N, Cin, H, W, Cout, stride, g,
-                                                                             static_cast<const bf16*>(w), dx);
-  conv3x3_bwd_weight_kernel<<<Cout * Cin, 256, 0, s>>>(N, Cin, H, W, Cout, stride, g, static_cast<const bf16*>(x), dw,
-                                                       db);
-  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
-}
-
-int lgb_nn_linear_forward(int N, int In, int Out, int relu, const void* x, const void* w, const float* b, void* y_bf16,
-                          float* y_f32, void* stream) {
-  if (N < 1 || In < 1 || Out < 1 || !x || !w || (!y_bf16 && !y_f32)) return LGB_ERR_INVALID_ARGUMENT;
-  dim3 grid((Out + 63) / 64, (N + 63) / 64);
-  gemm_kernel<bf16, bf16><<<grid, 256, 0, (cudaStream_t)stream>>>(
-      N, Out, In, static_cast<const bf16*>(x), In, 1, static_cast<const bf16*>(w), 1, In, y_f32, b, relu,
-      static_cast<bf16*>(y_bf16));
-  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
-}
-
-int lgb_nn_linear_backward(int N, int In, int Out, const void* x, const void* w, const float* g, float* dx, float* dw,
-                           float* db, void* stream) {
-  if (N < 1 || In < 1 || Out < 1 || !x || !w || !g || !dw) return LGB_ERR_INVALID_ARGUMENT;
-  cudaStream_t s = (cudaStream_t)stream;
-  if (dx) {
-    dim3 grid((In + 63) / 64, (N + 63) / 64);
-    gemm_kernel<float, bf16><<<grid, 256, 0, s>>>(N, In, Out, g, Out, 1, static_cast<const bf16*>(w), In, 1, dx,
-                                                  nullptr, 0, nullptr);
-  }
-  {
-    dim3 grid((In + 63) / 64, (Out + 63) / 64);
-    gemm_kernel<float, bf16><<<grid, 256, 0, s>>>(Out, In, N, g, 1, Out, static_cast<const bf16*>(x), In, 1, dw,
-                                                  nullptr, 0, nullptr);
-  }
-  if (db) colsum_kernel<<<(Out + 127) / 128, 128, 0, s>>>(N, Out, g, db);
-  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
-}
 
 int lgb_nn_relu_backward(long long n, const void* y, const float* dy, float* g, void* stream) {
   if (n < 1 || !y || !dy || !g) return LGB_ERR_INVALID_ARGUMENT;

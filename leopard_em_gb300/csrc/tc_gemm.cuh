@@ -195,6 +195,8 @@ struct TcGemmArgs {
   int k_chunks;  // K / 64
   int terms;     // 1: hi*hi only; 3: hi*hi + lo*hi + hi*lo
   int* err;      // LGB_ERR_DEVICE_TIMEOUT on a bounded-wait timeout
+  int kc_split;  // > 0: CTA z accumulates chunks [z*kc_split, (z+1)*kc_split) only (split K; the
+                 // epilogue then adds its partial sums atomically); 0: all chunks
 };
 
 template <int BN>
@@ -222,6 +224,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int warp = threadIdx.x >> 5;
   const int m_tile = blockIdx.y, n_tile = blockIdx.x;
   const int KC = g.k_chunks;
+  const int kc0 = g.kc_split > 0 ? (int)blockIdx.z * g.kc_split : 0;  // first chunk of this CTA
+  const int NK = g.kc_split > 0 ? min(KC - kc0, g.kc_split) : KC;     // chunks of this CTA (>= 1)
   const bool lo_terms = g.terms == 3;
 
   if (threadIdx.x == 0) {
@@ -244,7 +248,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const uint32_t stage_bytes = lo_terms ? (uint32_t)S::STAGE : (uint32_t)(S::A_BYTES + S::B_BYTES);
     auto load = [&](int kc) {
       uint8_t* st = base + (kc & 1) * S::STAGE;
-      const size_t ao = ((size_t)m_tile * KC + kc) * a_blk, bo = ((size_t)n_tile * KC + kc) * b_blk;
+      const size_t ao = ((size_t)m_tile * KC + kc0 + kc) * a_blk, bo = ((size_t)n_tile * KC + kc0 + kc) * b_blk;
       mbar_expect_tx(&full[kc & 1], stage_bytes);
       bulk_g2s(st, g.a_hi + ao, S::A_BYTES, &full[kc & 1]);
       bulk_g2s(st + 2 * S::A_BYTES, g.b_hi + bo, S::B_BYTES, &full[kc & 1]);
@@ -258,11 +262,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     int issued = 0, landed = 0;  // chunks whose copies were issued / have been waited for
     load(0);
     ++issued;
-    if (KC > 1) {
+    if (NK > 1) {
       load(1);
       ++issued;
     }
-    for (int kc = 0; kc < KC && ok; ++kc) {
+    for (int kc = 0; kc < NK && ok; ++kc) {
       const int s = kc & 1;
       if (!mbar_wait(&full[s], (kc >> 1) & 1)) {
         ok = false;
@@ -286,7 +290,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       mma_commit(&empty[s]);
       // chunk kc+1 goes into the stage of chunk kc-1 once that chunk's MMAs have
       // read it; chunk kc's MMAs keep the tensor pipe busy meanwhile
-      if (kc >= 1 && kc + 1 < KC) {
+      if (kc >= 1 && kc + 1 < NK) {
         if (!mbar_wait(&empty[(kc - 1) & 1], ((kc - 1) >> 1) & 1)) {
           ok = false;
           break;

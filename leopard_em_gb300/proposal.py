@@ -79,6 +79,26 @@ class ProposalNet:
         self.mb = [torch.zeros_like(b) for b in self.b]
         self.vb = [torch.zeros_like(b) for b in self.b]
         self.step_count = 0
+        self._ws = torch.empty(0, dtype=torch.uint8, device=self.dev)
+        self.device_status = torch.zeros(1, dtype=torch.int32, device=self.dev)
+
+    def _workspace(self, N: int, kind: str, cin: int, hw: int, cout: int, stride: int) -> torch.Tensor:
+        """Operand workspace of the tensor-core layers, grown to the largest layer seen."""
+        need = ctypes.c_size_t(0)
+        if kind == "conv":
+            check(lib().lgb_nn_conv3x3_workspace_size(N, cin, hw, hw, cout, stride, ctypes.byref(need)),
+                  "conv workspace")
+        else:
+            check(lib().lgb_nn_linear_workspace_size(N, cin, cout, ctypes.byref(need)), "linear workspace")
+        if self._ws.numel() < need.value:
+            self._ws = torch.empty(need.value, dtype=torch.uint8, device=self.dev)
+        return self._ws
+
+    def check_device_status(self) -> None:
+        """Raise if a bounded device wait of the tensor-core kernels ran out (synchronises)."""
+        st = int(self.device_status.item())
+        if st:
+            check(st, "proposal network kernels")
 
     @property
     def n_params(self) -> int:
@@ -98,16 +118,20 @@ class ProposalNet:
             if kind == "conv":
                 ho = (hw - 1) // stride + 1
                 y = torch.empty((N, cout, ho, ho), dtype=torch.bfloat16, device=self.dev)
+                ws = self._workspace(N, kind, cin, hw, cout, stride)
                 check(L.lgb_nn_conv3x3_forward(N, cin, hw, hw, cout, stride, int(relu), _p(a), _p(self.wbf[i]),
-                                               _p(self.b[i]), _p(y), s), "conv forward")
+                                               _p(self.b[i]), _p(y), _p(ws), ws.numel(), _p(self.device_status), s),
+                      "conv forward")
                 hw = ho
                 acts.append(y)
             else:
                 last = i == len(LAYERS) - 1
                 ybf = torch.empty((N, cout), dtype=torch.bfloat16, device=self.dev)
                 yf = torch.empty((N, cout), dtype=torch.float32, device=self.dev) if last else None
+                ws = self._workspace(N, kind, cin, 1, cout, 1)
                 check(L.lgb_nn_linear_forward(N, cin, cout, int(relu), _p(a), _p(self.wbf[i]), _p(self.b[i]),
-                                              _p(ybf), _p(yf), s), "linear forward")
+                                              _p(ybf), _p(yf), _p(ws), ws.numel(), _p(self.device_status), s),
+                      "linear forward")
                 acts.append(ybf)
                 out = yf
         self._acts = acts
@@ -134,13 +158,17 @@ class ProposalNet:
             need_dx = i > 0
             if kind == "fc":
                 dx = torch.empty((N, cin), dtype=torch.float32, device=self.dev) if need_dx else None
+                ws = self._workspace(N, kind, cin, 1, cout, 1)
                 check(L.lgb_nn_linear_backward(N, cin, cout, _p(x), _p(self.wbf[i]), _p(g), _p(dx), _p(self.gw[i]),
-                                               _p(self.gb[i]), s), "linear backward")
+                                               _p(self.gb[i]), _p(ws), ws.numel(), _p(self.device_status), s),
+                      "linear backward")
             else:
                 hw = sizes[i]
                 dx = torch.empty((N, cin, hw, hw), dtype=torch.float32, device=self.dev) if need_dx else None
+                ws = self._workspace(N, kind, cin, hw, cout, stride)
                 check(L.lgb_nn_conv3x3_backward(N, cin, hw, hw, cout, stride, _p(x), _p(self.wbf[i]), _p(g), _p(dx),
-                                                _p(self.gw[i]), _p(self.gb[i]), s), "conv backward")
+                                                _p(self.gw[i]), _p(self.gb[i]), _p(ws), ws.numel(),
+                                                _p(self.device_status), s), "conv backward")
             if need_dx:
                 g = dx.reshape(acts[i].shape) if LAYERS[i - 1][0] == "conv" and kind == "fc" else dx
 
@@ -267,6 +295,7 @@ def train(net: ProposalNet, inputs: torch.Tensor, targets: torch.Tensor, epochs:
             net.adam_step(cur)
             k += 1
     torch.cuda.synchronize(net.dev)
+    net.check_device_status()
     return TrainReport(k, float(loss.item()) if loss is not None else float("nan"), time.perf_counter() - t0,
                        k * batch)
 
@@ -275,6 +304,7 @@ def predict(net: ProposalNet, inputs: torch.Tensor, batch: int = 1024):
     outs = []
     for a in range(0, inputs.shape[0], batch):
         outs.append(net.forward(inputs[a : a + batch]))
+    net.check_device_status()
     return torch.cat(outs)
 
 
