@@ -5,13 +5,14 @@ Workload (production configuration): 4096 x 4096 micrograph (N(0,1) noise +
 300 planted projections at SNR 0.1), 384^3 Gaussian-blob template at
 1.06 A/px, 3 defocus planes (-200/0/+200 A around 10000 A), orientation grid
 2.5 deg out-of-plane / 1.5 deg in-plane (~1.58 M orientations), orientation
-batch 8.  All inputs are synthetic and seeded.
+batch 16 (the autotuner's choice for a 4096^2 grid).  All inputs are synthetic
+and seeded.
 
 One "step" = one chunk of ``--orient-per-step`` consecutive orientations of
-the grid (default 96 = 12 batches of 8 = 288 cross-correlograms), folded into
+the grid (default 96 = 6 batches of 16 = 288 cross-correlograms), folded into
 the running statistics maps, exactly as one slice of a full search.
 ``value``      orientations/s with inputs resident in HBM (device-timed, CUDA
-               events on the launching stream); every step streams a 1.6 GB
+               events on the launching stream); every batch streams a 3.2 GB
                correlogram intermediate, far larger than the 129 MB L2.
 ``e2e``        the same metric through the public drop-in
                ``core_match_template`` called with pinned host tensors: every
@@ -829,9 +830,11 @@ def main():
     peaks, peak_kind = _peaks()
     per_launch_ms = stage_ms[top] / max(1, launches[top])
     ach = alg_bytes.get(top, 0.0) / (per_launch_ms / 1e3) / 1e9 if top in alg_bytes else None
-    # DRAM bytes (read + write) of one launch, from an ncu capture of this
-    # workload at batch 8 (dram__bytes_read.sum + dram__bytes_write.sum)
-    measured_traffic = {("production", 8, "colpass"): 1.875e9, ("production", 8, "rowpass"): 2.390e9}
+    # DRAM bytes (read + write) of one launch, from ncu captures of this
+    # workload (dram__bytes_read.sum + dram__bytes_write.sum; one launch each,
+    # --set full) at orientation batch 8 and 16
+    measured_traffic = {("production", 8, "colpass"): 1.875e9, ("production", 8, "rowpass"): 2.390e9,
+                        ("production", 16, "colpass"): 3.657e9, ("production", 16, "rowpass"): 4.042e9}
     roofline = {
         "bound": "hbm", "kernel": top, "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
         "frac": (ach / peaks["hbm_gbs"]) if ach else None,
@@ -926,7 +929,8 @@ def main():
             "config": {"workload": cfg.name, "image": [H, W], "template": d, "defocus_planes": n_cd,
                        "orientation_batch": B, "orientations_per_step": chunk, "orientations_total": N,
                        "cross_correlations_per_s": value * n_cd,
-                       "l2": "inputs larger than L2 (1.6 GB correlogram intermediate per batch)",
+                       "l2": f"inputs larger than L2 ({8 * n_cd * B * H * (W // 2 + 1) / 1e9:.1f} GB correlogram "
+                             "intermediate per batch)",
                        "parallelism": f"orientation-sharded x{world}"},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "orientations_per_call": e2e_chunk, "two_run_model": two_run,
