@@ -685,8 +685,7 @@ def learned_refine_bench(kw, dev, cfg, plain_res, n_plain):
     path = os.path.join(ROOT, "leopard_em_gb300", "weights", "proposal_refine288.npz")
     if not os.path.exists(path):
         return {"learned": None}
-    net = pr.ProposalNet(dev)
-    pr.load_weights(net, path)
+    net = pr.load_net(path, dev)
     # +-0.5 deg at 0.125 deg: the same 576 offsets as +-1 deg at 0.25 deg, finer
     # (the proposals are within ~0.2 deg)
     small = sy.local_euler_offsets(0.5, 0.125, 0.5, 0.125)

@@ -415,8 +415,8 @@ struct RowFused {
   static size_t smem(int wcp) { return sizeof(float2) * (size_t)(2 * wcp + ZS + TAB); }
 };
 
-template <int WH, int NT, class RL>
-__global__ void __launch_bounds__(NT, 3)
+template <int WH, int NT, class RL, int MINB = 3>
+__global__ void __launch_bounds__(NT, MINB)
     rowpass_fused_kernel(const float2* __restrict__ Y, int y_rows, int Wcp, int n_c, int nb, int n_orient, int o0,
                          const int* __restrict__ o0_dev, float scale, float* __restrict__ mip,
                          int* __restrict__ best, double* __restrict__ s1, double* __restrict__ s2) {

@@ -355,12 +355,17 @@ __global__ void __launch_bounds__(ROWS * 16)
   constexpr int WH = 144;  // W / 2
   constexpr int C2 = 8;    // c2r: M = 16 x 8
   constexpr int R2 = 9;    // rfft: WH = 16 x 9
-  constexpr int ZR = IdxPad16::pad(WH) + 2;
-  static_assert(ZR >= WC + 1, "staged row fits the rfft buffer");
+  // Row strides of the shared buffers, chosen for the densely packed first
+  // passes below, where two rows share a half-warp: 152 float2 (xz) and
+  // 153 = R2 * S1 (zb) keep those loads and stores at the fewest bank
+  // conflicts the index maps allow (per-row passes are conflict free at any
+  // stride).
+  constexpr int ZR = 152;
+  static_assert(ZR >= IdxPad16::pad(WH) - 1 && ZR >= WC + 1, "staged row and padded rfft input fit");
   // xin (the staged row of T, read only by c2r pass 1) and zr (the rfft input,
   // written from c2r pass 2 on, then Z) share one buffer per row
   __shared__ float2 xz[ROWS][ZR];
-  __shared__ float2 zb[ROWS][R2 * S1 + 1];  // c2r transpose (8 x 17), then rfft transpose (9 x 17)
+  __shared__ float2 zb[ROWS][R2 * S1];  // c2r transpose (8 x 17), then rfft transpose (9 x 17)
   float2(*xin)[ZR] = xz;
   float2(*zr)[ZR] = xz;
   __shared__ float2 pre[M];                 // exp(+i pi k / M)
@@ -394,14 +399,18 @@ __global__ void __launch_bounds__(ROWS * 16)
     const float2 v = post[2 * m <= WH ? 2 * m : 2 * m - WH];
     rootr[m] = 2 * m <= WH ? v : make_float2(-v.x, -v.y);
   }
-  // ---- c2r pass 1 (radix 16) on the pre-twiddled z[k], k = t + 8q
-  if (t < C2) {
+  // The two radix-16 passes have fewer DFTs per row (8 and 9) than a row has
+  // threads (16): their (row, DFT) tasks are packed densely onto the CTA's
+  // threads, so whole warps idle instead of half of every warp's lanes.
+  // ---- c2r pass 1 (radix 16) on the pre-twiddled z[k], k = tt + 8q
+  if (threadIdx.x < ROWS * C2) {
+    const int gg = threadIdx.x / C2, tt = threadIdx.x - (threadIdx.x / C2) * C2;
     float2 v[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
-      const int k = t + q * C2;
-      float2 a = xin[g][k];
-      float2 b = xin[g][M - k];
+      const int k = tt + q * C2;
+      float2 a = xin[gg][k];
+      float2 b = xin[gg][M - k];
       if (k == 0) { a.y = 0.f; b.y = 0.f; }  // DC and Nyquist: real parts only
       b.y = -b.y;
       const float2 xo = cmul(csub(a, b), pre[k]);
@@ -409,7 +418,7 @@ __global__ void __launch_bounds__(ROWS * 16)
     }
     Dft<16, +1>::run(v);
 #pragma unroll
-    for (int q = 0; q < 16; ++q) zb[g][t * S1 + q] = v[q];
+    for (int q = 0; q < 16; ++q) zb[gg][tt * S1 + q] = v[q];
   }
   __syncthreads();
   // ---- c2r pass 2 (radix 8): pixel pairs m = t + 16r, moments, shifted rfft input
@@ -453,14 +462,15 @@ __global__ void __launch_bounds__(ROWS * 16)
     }
   }
   __syncthreads();
-  // ---- rfft pass 1 (radix 16) over m' = t + 9q
-  if (t < R2) {
+  // ---- rfft pass 1 (radix 16) over m' = tt + 9q, tasks packed as above
+  if (threadIdx.x < ROWS * R2) {
+    const int gg = threadIdx.x / R2, tt = threadIdx.x - (threadIdx.x / R2) * R2;
     float2 v[16];
 #pragma unroll
-    for (int q = 0; q < 16; ++q) v[q] = zr[g][IdxPad16::f(t + q * R2)];
+    for (int q = 0; q < 16; ++q) v[q] = zr[gg][IdxPad16::f(tt + q * R2)];
     Dft<16, -1>::run(v);
 #pragma unroll
-    for (int q = 0; q < 16; ++q) zb[g][t * S1 + q] = v[q];
+    for (int q = 0; q < 16; ++q) zb[gg][tt * S1 + q] = v[q];
   }
   __syncthreads();
   // ---- rfft pass 2 (radix 9): Z[t + 16r]

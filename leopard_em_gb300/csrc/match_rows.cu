@@ -96,19 +96,19 @@ int launch_pad_rfft(int W, const float* proj, const double* rowstats, int h, int
   }
 }
 
-template <int WH, int NT, class RL>
+template <int WH, int NT, class RL, int MINB = 3>
 static int rowpass_fused_t(const void* Y, int H, int y_rows, int Wcp, int n_c, int nb, int n_orient, int o0,
                            const int* o0_dev, float* mip, int* best, double* s1, double* s2, cudaStream_t s) {
   using RF = RowFused<WH, NT, RL>;
   if (n_c > 0xffff) return LGB_ERR_INVALID_ARGUMENT;  // batch indices are kept in 16 bits
   const size_t smem = RF::smem(Wcp);
-  if (cudaFuncSetAttribute(rowpass_fused_kernel<WH, NT, RL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (cudaFuncSetAttribute(rowpass_fused_kernel<WH, NT, RL, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem) != cudaSuccess ||
-      cudaFuncSetAttribute(rowpass_fused_kernel<WH, NT, RL>, cudaFuncAttributePreferredSharedMemoryCarveout,
+      cudaFuncSetAttribute(rowpass_fused_kernel<WH, NT, RL, MINB>, cudaFuncAttributePreferredSharedMemoryCarveout,
                            cudaSharedmemCarveoutMaxShared) != cudaSuccess)
     return LGB_ERR_CUDA;
   const float scale = 1.0f / ((float)H * (float)(2 * WH));
-  rowpass_fused_kernel<WH, NT, RL><<<y_rows, NT, smem, s>>>(static_cast<const float2*>(Y), y_rows, Wcp, n_c, nb,
+  rowpass_fused_kernel<WH, NT, RL, MINB><<<y_rows, NT, smem, s>>>(static_cast<const float2*>(Y), y_rows, Wcp, n_c, nb,
                                                             n_orient, o0, o0_dev, scale, mip, best, s1, s2);
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
@@ -120,6 +120,9 @@ int launch_rowpass(int W, const void* Y, int H, int y_rows, int Wcp, int n_c, in
     case 2048:
       return rowpass_fused_t<2048, 256, Radices<8, 8, 8, 4>>(Y, H, y_rows, Wcp, n_c, nb, n_orient, o0, o0_dev, mip,
                                                              best, s1, s2, s);
+    case 2880:  // 5760-wide grids (e.g. a 5760 x 4092 micrograph searched transposed); 2 CTAs per SM
+      return rowpass_fused_t<2880, 360, Radices<8, 9, 5, 8>, 2>(Y, H, y_rows, Wcp, n_c, nb, n_orient, o0, o0_dev,
+                                                                mip, best, s1, s2, s);
     case 1024:
       return rowpass_fused_t<1024, 256, Radices<8, 8, 4, 4>>(Y, H, y_rows, Wcp, n_c, nb, n_orient, o0, o0_dev, mip,
                                                              best, s1, s2, s);

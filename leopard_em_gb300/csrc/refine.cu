@@ -192,8 +192,12 @@ __global__ void __launch_bounds__(ROWS* R1)
                                unsigned long long* __restrict__ slot_key, unsigned* __restrict__ slot_cc) {
   constexpr int WH = R1 * R2, NT = R1, S1 = R1 + 1, NROOT = (R1 - 1) * (R2 - 1) + 1;
   static_assert(R1 >= R2, "second pass uses every thread of the row");
-  __shared__ float2 xr[ROWS][WH + 2];
-  __shared__ float2 zb[ROWS][R2 * S1 + 1];
+  // row strides 9 (mod 16) float2: the first pass packs rows two to a
+  // half-warp, and this stride keeps their loads and stores conflict free
+  constexpr int XS = WH + 1 + ((9 - (WH + 1) % 16) + 16) % 16;
+  constexpr int ZS = R2 * S1 + ((9 - (R2 * S1) % 16) + 16) % 16;
+  __shared__ float2 xr[ROWS][XS];
+  __shared__ float2 zb[ROWS][ZS];
   __shared__ float2 pre[WH];      // exp(+i pi k / WH)
   __shared__ float2 root[NROOT];  // exp(+2 pi i m / WH)
   __shared__ unsigned long long red_key[1];
@@ -229,13 +233,16 @@ __global__ void __launch_bounds__(ROWS* R1)
       for (int k = t; k <= WH; k += NT) xr[g][k] = row[k];
     }
     __syncthreads();
-    if (act && t < R2) {
+    // first pass: R2 (< R1) DFTs per row, the (row, DFT) tasks packed densely
+    // onto the CTA's threads so that whole warps idle instead of lanes
+    if (threadIdx.x < ROWS * R2 && cb + (int)threadIdx.x / R2 < c_end) {
+      const int gg = threadIdx.x / R2, tt = threadIdx.x - (threadIdx.x / R2) * R2;
       float2 v[R1];
 #pragma unroll
       for (int q = 0; q < R1; ++q) {
-        const int k = t + q * R2;
-        float2 A = xr[g][k];
-        float2 B = xr[g][WH - k];
+        const int k = tt + q * R2;
+        float2 A = xr[gg][k];
+        float2 B = xr[gg][WH - k];
         if (k == 0) { A.y = 0.f; B.y = 0.f; }
         B.y = -B.y;
         const float2 xo = cmul(csub(A, B), pre[k]);
@@ -243,7 +250,7 @@ __global__ void __launch_bounds__(ROWS* R1)
       }
       Dft<R1, +1>::run(v);
 #pragma unroll
-      for (int q = 0; q < R1; ++q) zb[g][t * S1 + q] = v[q];
+      for (int q = 0; q < R1; ++q) zb[gg][tt * S1 + q] = v[q];
     }
     __syncthreads();
     if (act) {

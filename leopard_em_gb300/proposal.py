@@ -23,6 +23,7 @@ than the neighbourhood of the starting pose.
 from __future__ import annotations
 
 import ctypes
+import json
 import math
 from dataclasses import dataclass
 
@@ -50,6 +51,26 @@ ROT_SCALE = math.radians(3.0)  # 6D-delta targets are (col - identity) / ROT_SCA
 DEFOCUS_SCALE = 400.0          # defocus-offset target in units of 400 A
 
 
+def _check_layers(layers) -> None:
+    """Convolutions first (BAND x BAND input, CHANNELS channels, <= 128
+    channels each), then linear layers; the first linear layer takes the
+    flattened last feature map; the last layer has 7 outputs."""
+    hw, ch, seen_fc = BAND, CHANNELS, False
+    for kind, cin, cout, stride, _ in layers:
+        if kind == "conv":
+            if seen_fc or cin != ch or not 1 <= cout <= 128 or stride not in (1, 2):
+                raise ValueError(f"bad convolution layer {(kind, cin, cout, stride)}")
+            hw, ch = (hw - 1) // stride + 1, cout
+        elif kind == "fc":
+            if cin != (ch * hw * hw if not seen_fc else ch):
+                raise ValueError(f"linear layer input {cin} does not match the previous layer's {ch}x{hw}x{hw}")
+            seen_fc, ch, hw = True, cout, 1
+        else:
+            raise ValueError(f"unknown layer kind {kind!r}")
+    if ch != 7:
+        raise ValueError("the last layer must have 7 outputs")
+
+
 def _stream(dev):
     return ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
 
@@ -61,11 +82,13 @@ def _p(t):
 class ProposalNet:
     """Parameters, activations and optimizer state of the proposal CNN."""
 
-    def __init__(self, device, seed: int = 0):
+    def __init__(self, device, seed: int = 0, layers=None):
         self.dev = torch.device(device)
+        self.layers = [tuple(l) for l in (layers if layers is not None else LAYERS)]
+        _check_layers(self.layers)
         g = torch.Generator().manual_seed(seed)
         self.w, self.b = [], []
-        for kind, cin, cout, _, _ in LAYERS:
+        for kind, cin, cout, _, _ in self.layers:
             fan_in = cin * 9 if kind == "conv" else cin
             shape = (cout, cin, 3, 3) if kind == "conv" else (cout, cin)
             self.w.append((torch.randn(shape, generator=g) * math.sqrt(2.0 / fan_in)).to(self.dev))
@@ -113,7 +136,7 @@ class ProposalNet:
         acts = [x.contiguous()]
         hw = BAND
         out = None
-        for i, (kind, cin, cout, stride, relu) in enumerate(LAYERS):
+        for i, (kind, cin, cout, stride, relu) in enumerate(self.layers):
             a = acts[-1]
             if kind == "conv":
                 ho = (hw - 1) // stride + 1
@@ -125,7 +148,7 @@ class ProposalNet:
                 hw = ho
                 acts.append(y)
             else:
-                last = i == len(LAYERS) - 1
+                last = i == len(self.layers) - 1
                 ybf = torch.empty((N, cout), dtype=torch.bfloat16, device=self.dev)
                 yf = torch.empty((N, cout), dtype=torch.float32, device=self.dev) if last else None
                 ws = self._workspace(N, kind, cin, 1, cout, 1)
@@ -145,11 +168,11 @@ class ProposalNet:
         N = dout.shape[0]
         g = dout.contiguous()
         sizes = [BAND]
-        for kind, _, _, stride, _ in LAYERS:
+        for kind, _, _, stride, _ in self.layers:
             if kind == "conv":
                 sizes.append((sizes[-1] - 1) // stride + 1)
-        for i in range(len(LAYERS) - 1, -1, -1):
-            kind, cin, cout, stride, relu = LAYERS[i]
+        for i in range(len(self.layers) - 1, -1, -1):
+            kind, cin, cout, stride, relu = self.layers[i]
             if relu:
                 gg = torch.empty_like(g)
                 check(L.lgb_nn_relu_backward(g.numel(), _p(acts[i + 1]), _p(g), _p(gg), s), "relu backward")
@@ -170,13 +193,13 @@ class ProposalNet:
                                                 _p(self.gw[i]), _p(self.gb[i]), _p(ws), ws.numel(),
                                                 _p(self.device_status), s), "conv backward")
             if need_dx:
-                g = dx.reshape(acts[i].shape) if LAYERS[i - 1][0] == "conv" and kind == "fc" else dx
+                g = dx.reshape(acts[i].shape) if self.layers[i - 1][0] == "conv" and kind == "fc" else dx
 
     def adam_step(self, lr: float, weight_decay: float = 0.0) -> None:
         L = lib()
         s = _stream(self.dev)
         self.step_count += 1
-        for i in range(len(LAYERS)):
+        for i in range(len(self.layers)):
             check(L.lgb_nn_adam(self.w[i].numel(), _p(self.w[i]), _p(self.gw[i]), _p(self.mw[i]), _p(self.vw[i]),
                                 _p(self.wbf[i]), lr, 0.9, 0.999, 1e-8, weight_decay, self.step_count, s), "adam w")
             check(L.lgb_nn_adam(self.b[i].numel(), _p(self.b[i]), _p(self.gb[i]), _p(self.mb[i]), _p(self.vb[i]),
@@ -196,7 +219,10 @@ class ProposalNet:
             f"b{i}": b.cpu().numpy() for i, b in enumerate(self.b)}
 
     def load(self, state: dict) -> None:
-        for i in range(len(LAYERS)):
+        for i in range(len(self.layers)):
+            if tuple(state[f"w{i}"].shape) != tuple(self.w[i].shape):
+                raise ValueError(f"layer {i}: stored weights {tuple(state[f'w{i}'].shape)} do not fit "
+                                 f"{tuple(self.w[i].shape)}")
             self.w[i].copy_(torch.from_numpy(np.asarray(state[f"w{i}"])).to(self.dev))
             self.b[i].copy_(torch.from_numpy(np.asarray(state[f"b{i}"])).to(self.dev))
             self.wbf[i] = self.w[i].to(torch.bfloat16)
@@ -372,8 +398,24 @@ def refine_with_proposals(net: ProposalNet | None, kwargs: dict, device, small_o
 
 def load_weights(net: ProposalNet, path: str) -> None:
     with np.load(path) as z:
-        net.load({k: z[k].astype(np.float32) for k in z.files})
+        net.load({k: z[k].astype(np.float32) for k in z.files if k != "layers"})
+
+
+def stored_layers(path: str):
+    """The layer list saved with the weights (files without one hold LAYERS)."""
+    with np.load(path) as z:
+        if "layers" not in z.files:
+            return list(LAYERS)
+        return [(k, int(a), int(b), int(s), bool(r)) for k, a, b, s, r in json.loads(str(z["layers"]))]
+
+
+def load_net(path: str, device) -> ProposalNet:
+    """A network built from the layer list stored with the weights, weights loaded."""
+    net = ProposalNet(device, layers=stored_layers(path))
+    load_weights(net, path)
+    return net
 
 
 def save_weights(net: ProposalNet, path: str) -> None:
-    np.savez_compressed(path, **{k: v.astype(np.float16) for k, v in net.state().items()})
+    np.savez_compressed(path, layers=np.array(json.dumps([list(l) for l in net.layers])),
+                        **{k: v.astype(np.float16) for k, v in net.state().items()})

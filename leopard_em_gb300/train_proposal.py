@@ -70,6 +70,11 @@ def main():
     ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--out", required=True)
+    ap.add_argument("--layers", default=None,
+                    help="JSON list of [kind, in, out, stride, relu] layers (default: proposal.LAYERS)")
+    ap.add_argument("--compare-layers", default=None,
+                    help="JSON layer list of a second network trained on the same data for comparison")
+    ap.add_argument("--compare-out", default=None, help="where to save the second network's weights")
     args = ap.parse_args()
     dev = torch.device("cuda:0")
     cfg = sy.CONFIG_REFINE
@@ -77,13 +82,19 @@ def main():
     x, t, _ = build_dataset(cfg, args.n_train, 1000, dev)
     x_te, _, truth = build_dataset(cfg, args.n_test, 10 ** 8, dev)
     t_data = time.perf_counter() - t0
-    net = pr.ProposalNet(dev, seed=0)
-    rep = pr.train(net, x, t, epochs=args.epochs, batch=args.batch, lr=args.lr)
-    pr.save_weights(net, args.out)
-    ev = evaluate(net, x_te, truth)
-    print(json.dumps({"n_train": args.n_train, "epochs": args.epochs, "params": net.n_params,
-                      "data_seconds": t_data, "train_seconds": rep.seconds, "steps": rep.steps,
-                      "final_loss": rep.final_loss, "held_out": ev}))
+    runs = [(args.layers, args.out)]
+    if args.compare_layers:
+        runs.append((args.compare_layers, args.compare_out))
+    for spec, out in runs:
+        layers = json.loads(spec) if spec else None
+        net = pr.ProposalNet(dev, seed=0, layers=layers)
+        rep = pr.train(net, x, t, epochs=args.epochs, batch=args.batch, lr=args.lr)
+        if out:
+            pr.save_weights(net, out)
+        ev = evaluate(net, x_te, truth)
+        print(json.dumps({"n_train": args.n_train, "epochs": args.epochs, "layers": net.layers,
+                          "params": net.n_params, "data_seconds": t_data, "train_seconds": rep.seconds,
+                          "steps": rep.steps, "final_loss": rep.final_loss, "held_out": ev}), flush=True)
 
 
 if __name__ == "__main__":

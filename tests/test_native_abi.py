@@ -71,3 +71,27 @@ def test_ctypes_signatures_match_header_arity(lib):
         n = 0 if params in ("void", "") else len(params.split(","))
         assert name in _native._SIGNATURES, name
         assert len(_native._SIGNATURES[name][0]) == n, name
+
+
+def test_network_layer_validation_without_gpu(lib):
+    """The tensor-core layer entry points check shapes, workspace size and
+    alignment before any device call."""
+    sz = ctypes.c_size_t(0)
+    ok, bad, small = _native.LGB_OK, _native.LGB_ERR_INVALID_ARGUMENT, _native.LGB_ERR_WORKSPACE_TOO_SMALL
+    assert lib.lgb_nn_conv3x3_workspace_size(4, 12, 64, 64, 32, 2, ctypes.byref(sz)) == ok
+    # forward operands: im2col (4*32*32 pixels padded to 128) x (12*9 padded to 64) + weights, BF16
+    assert sz.value >= (4096 * 128 + 32 * 128) * 2
+    need = sz.value
+    for args in [(4, 12, 64, 64, 129, 2), (4, 12, 64, 64, 32, 3), (0, 12, 64, 64, 32, 2), (4, 129, 8, 8, 32, 1)]:
+        assert lib.lgb_nn_conv3x3_workspace_size(*args, ctypes.byref(sz)) == bad, args
+    p = ctypes.c_void_p(1 << 20)  # never dereferenced: every check below fails before a device call
+    assert lib.lgb_nn_conv3x3_forward(4, 12, 64, 64, 32, 2, 1, p, p, None, p, p, need - 1, p, None) == small
+    assert lib.lgb_nn_conv3x3_forward(4, 12, 64, 64, 32, 2, 1, p, p, None, p, ctypes.c_void_p((1 << 20) + 16),
+                                      need, p, None) == bad  # workspace not 256-byte aligned
+    assert lib.lgb_nn_conv3x3_forward(4, 12, 64, 64, 32, 2, 1, p, p, None, p, p, need, None, None) == bad
+    assert lib.lgb_nn_conv3x3_backward(4, 12, 64, 64, 32, 2, p, p, p, None, p, None, p, need - 1, p, None) == small
+    assert lib.lgb_nn_linear_workspace_size(256, 2048, 512, ctypes.byref(sz)) == ok
+    assert sz.value >= (512 * 2048 + 256 * 2048) * 2
+    assert lib.lgb_nn_linear_workspace_size(256, 0, 512, ctypes.byref(sz)) == bad
+    assert lib.lgb_nn_linear_forward(256, 2048, 512, 1, p, p, None, None, None, p, 1 << 30, p, None) == bad  # no output
+    assert lib.lgb_nn_linear_backward(256, 2048, 512, p, p, p, None, p, None, p, 16, p, None) == small

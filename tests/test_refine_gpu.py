@@ -129,8 +129,7 @@ def test_learned_proposals_match_plain_grid_snr_with_fewer_correlations():
     dev = torch.device("cuda:0")
     kw, _ = sy.make_refine_workload(cfg, 128, device=dev, seed_offset=777)
     plain = core_refine_template(**kw, device=dev, batch_size=cfg.batch)
-    net = pr.ProposalNet(dev)
-    pr.load_weights(net, path)
+    net = pr.load_net(path, dev)
     small = sy.local_euler_offsets(0.5, 0.125, 0.5, 0.125)
     small_df = torch.arange(-100.0, 100.0 + 1e-6, 50.0)
     res, info = pr.refine_with_proposals(net, kw, dev, small, small_df, batch_size=cfg.batch)
