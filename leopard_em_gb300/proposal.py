@@ -1,6 +1,6 @@
 """Learned orientation / defocus proposals for the local refinement.
 
-A BF16 CNN (5 conv + 3 linear layers, ~1.45 M parameters) sees, per particle,
+A BF16 CNN (5 conv + 3 linear layers, 3.11 M parameters) sees, per particle,
 the low-frequency band of its spectrum (shift-aligned to the reference), the
 template's central slice at its starting pose on the same band, and that
 reference's derivatives for small rotations about the three image axes and
@@ -9,7 +9,8 @@ which the network learns -- and predicts the
 rotation that takes the starting pose to the particle's pose (6D
 representation: the first two columns of the delta rotation, applied on the
 left like the refinement offsets) and the defocus offset.  Every layer's
-forward and backward pass and the Adam update are this package's CUDA kernels
+forward and backward pass runs on the tcgen05 tensor cores (``csrc/nn_tc.cu``),
+the Adam update and the input builder are this package's CUDA kernels
 (``csrc/nn.cu``); torch only holds device memory.
 
 The network is trained only on particles produced by the method's own
@@ -38,14 +39,14 @@ IMAGE_CHANNELS = 6  # particle, reference, d/d(rot x, y, z), d/d(defocus)
 CHANNELS = 12       # + constant maps of the Gauss-Newton step (shift x, y, rot x, y, z, defocus)
 # (kind, in, out, stride, relu); conv input spatial sizes 64 -> 32 -> 16 -> 8 -> 4 -> 4
 LAYERS = [
-    ("conv", CHANNELS, 32, 2, True),
-    ("conv", 32, 64, 2, True),
-    ("conv", 64, 96, 2, True),
+    ("conv", CHANNELS, 48, 2, True),
+    ("conv", 48, 96, 2, True),
     ("conv", 96, 128, 2, True),
+    ("conv", 128, 128, 2, True),
     ("conv", 128, 128, 1, True),
-    ("fc", 128 * 4 * 4, 512, 1, True),
-    ("fc", 512, 128, 1, True),
-    ("fc", 128, 7, 1, False),
+    ("fc", 128 * 4 * 4, 1152, 1, True),
+    ("fc", 1152, 256, 1, True),
+    ("fc", 256, 7, 1, False),
 ]
 ROT_SCALE = math.radians(3.0)  # 6D-delta targets are (col - identity) / ROT_SCALE
 DEFOCUS_SCALE = 400.0          # defocus-offset target in units of 400 A
