@@ -298,14 +298,14 @@ struct EpiLinDx {
 template <class Epi, int BN>
 static int run_gemm(int m_tiles, int n_tiles, int k_chunks, int splits, const uint16_t* a, const uint16_t* b,
                     int* status, const typename Epi::Params& ep, cudaStream_t s) {
-  constexpr int SMEM = TcSmem<BN>::BYTES;
-  if (cudaFuncSetAttribute(tc_gemm_kernel<Epi, BN, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM) !=
-      cudaSuccess)
+  constexpr int SMEM = TcSmem<BN, false>::BYTES;  // single BF16 term: no lo buffers
+  if (cudaFuncSetAttribute(tc_gemm_kernel<Epi, BN, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           SMEM) != cudaSuccess)
     return LGB_ERR_CUDA;
   const int per = (k_chunks + splits - 1) / splits;
   const int z = (k_chunks + per - 1) / per;
   TcGemmArgs g{a, nullptr, b, nullptr, k_chunks, 1, status, splits > 1 ? per : 0};
-  tc_gemm_kernel<Epi, BN, false><<<dim3(n_tiles, m_tiles, z), kTcThreads, SMEM, s>>>(g, ep);
+  tc_gemm_kernel<Epi, BN, false, false><<<dim3(n_tiles, m_tiles, z), kTcThreads, SMEM, s>>>(g, ep);
   return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 

@@ -199,20 +199,24 @@ struct TcGemmArgs {
                  // epilogue then adds its partial sums atomically); 0: all chunks
 };
 
-template <int BN>
+// Shared memory of one CTA: two pipeline stages of [A hi | A lo | B hi | B lo]
+// K chunks, or [A hi | B hi] when the kernel is built without lo terms (LO =
+// false: half the footprint, so more CTAs fit an SM for single-term GEMMs).
+template <int BN, bool LO = true>
 struct TcSmem {
   static constexpr int A_BYTES = kTcM * kTcKC * 2;  // 16 KB
   static constexpr int B_BYTES = BN * kTcKC * 2;
-  static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;
+  static constexpr int B_OFF = (LO ? 2 : 1) * A_BYTES;  // B hi within a stage
+  static constexpr int STAGE = (LO ? 2 : 1) * (A_BYTES + B_BYTES);
   static constexpr int STAGES = 2;
   static constexpr int BYTES = STAGES * STAGE + 1024 /* alignment */ + 128 /* barriers */;
 };
 
-template <class Epi, int BN, bool F16>
+template <class Epi, int BN, bool F16, bool LO = true>
 __global__ void __launch_bounds__(kTcThreads, 1)
     tc_gemm_kernel(TcGemmArgs g, typename Epi::Params ep) {
   static_assert(BN % 32 == 0 && BN >= 32 && BN <= 256, "N tile");
-  using S = TcSmem<BN>;
+  using S = TcSmem<BN, LO>;
   extern __shared__ uint8_t tc_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) & ~(uintptr_t)1023);
   uint64_t* full = reinterpret_cast<uint64_t*>(base + S::STAGES * S::STAGE);
@@ -226,7 +230,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int KC = g.k_chunks;
   const int kc0 = g.kc_split > 0 ? (int)blockIdx.z * g.kc_split : 0;  // first chunk of this CTA
   const int NK = g.kc_split > 0 ? min(KC - kc0, g.kc_split) : KC;     // chunks of this CTA (>= 1)
-  const bool lo_terms = g.terms == 3;
+  const bool lo_terms = LO && g.terms == 3;  // built without lo buffers: hi*hi only
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < 2; ++i) {
@@ -251,10 +255,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const size_t ao = ((size_t)m_tile * KC + kc0 + kc) * a_blk, bo = ((size_t)n_tile * KC + kc0 + kc) * b_blk;
       mbar_expect_tx(&full[kc & 1], stage_bytes);
       bulk_g2s(st, g.a_hi + ao, S::A_BYTES, &full[kc & 1]);
-      bulk_g2s(st + 2 * S::A_BYTES, g.b_hi + bo, S::B_BYTES, &full[kc & 1]);
+      bulk_g2s(st + S::B_OFF, g.b_hi + bo, S::B_BYTES, &full[kc & 1]);
       if (lo_terms) {
         bulk_g2s(st + S::A_BYTES, g.a_lo + ao, S::A_BYTES, &full[kc & 1]);
-        bulk_g2s(st + 2 * S::A_BYTES + S::B_BYTES, g.b_lo + bo, S::B_BYTES, &full[kc & 1]);
+        bulk_g2s(st + S::B_OFF + S::B_BYTES, g.b_lo + bo, S::B_BYTES, &full[kc & 1]);
       }
     };
     const uint32_t idesc = mma_idesc(kTcM, BN, F16);
@@ -275,7 +279,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       ++landed;
       tc_fence_after();
       const uint32_t sa = smem_u32(base + s * S::STAGE);
-      const uint32_t sb = sa + 2 * S::A_BYTES;
+      const uint32_t sb = sa + S::B_OFF;
       // term order: hi*hi, lo(A)*hi(B), hi(A)*lo(B)
       for (int t = 0; t < (lo_terms ? 3 : 1); ++t) {
         const uint32_t a0 = sa + (t == 1 ? S::A_BYTES : 0);

@@ -120,3 +120,94 @@ def test_trained_network_improves_on_starting_poses():
           f"defocus error {dferr_start:.1f} -> {dferr_prop:.1f} A")
     assert err_prop < 0.8 * err_start
     assert dferr_prop < 0.8 * dferr_start
+
+
+def _layer_ws(L, fn, *args):
+    import ctypes
+
+    n = ctypes.c_size_t(0)
+    assert fn(*args, ctypes.byref(n)) == 0
+    return torch.empty(n.value, dtype=torch.uint8, device=DEV)
+
+
+@pytest.mark.parametrize("N,Cin,H,Cout,stride", [(3, 5, 13, 7, 1), (2, 12, 17, 33, 2), (1, 128, 6, 128, 1),
+                                                 (5, 3, 31, 64, 2)])
+def test_conv_layer_odd_shapes_match_torch(N, Cin, H, Cout, stride):
+    """Tensor-core conv3x3 (forward, input, weight and bias gradients) on shapes
+    that fill no tile evenly, against torch's FP32 convolution of the same
+    BF16-rounded operands.  Tolerance 1e-2 relative: the output gradient enters
+    the MMA rounded to BF16."""
+    import ctypes
+
+    from leopard_em_gb300._native import lib
+
+    L = lib()
+    g = torch.Generator().manual_seed(N * 100 + Cin)
+    x = torch.randn(N, Cin, H, H, generator=g).to(torch.bfloat16)
+    w = (0.2 * torch.randn(Cout, Cin, 3, 3, generator=g)).to(torch.bfloat16)
+    b = torch.randn(Cout, generator=g)
+    Ho = (H - 1) // stride + 1
+    gy = torch.randn(N, Cout, Ho, Ho, generator=g)
+    xd, wd, bd, gd = x.to(DEV), w.to(DEV), b.to(DEV), gy.to(DEV)
+    ws = _layer_ws(L, L.lgb_nn_conv3x3_workspace_size, N, Cin, H, H, Cout, stride)
+    st = torch.zeros(1, dtype=torch.int32, device=DEV)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    y = torch.empty(N, Cout, Ho, Ho, dtype=torch.bfloat16, device=DEV)
+    assert L.lgb_nn_conv3x3_forward(N, Cin, H, H, Cout, stride, 0, xd.data_ptr(), wd.data_ptr(), bd.data_ptr(),
+                                    y.data_ptr(), ws.data_ptr(), ws.numel(), st.data_ptr(), s) == 0
+    dx = torch.empty(N, Cin, H, H, device=DEV)
+    dw = torch.empty(Cout, Cin, 3, 3, device=DEV)
+    db = torch.empty(Cout, device=DEV)
+    assert L.lgb_nn_conv3x3_backward(N, Cin, H, H, Cout, stride, xd.data_ptr(), wd.data_ptr(), gd.data_ptr(),
+                                     dx.data_ptr(), dw.data_ptr(), db.data_ptr(), ws.data_ptr(), ws.numel(),
+                                     st.data_ptr(), s) == 0
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0
+    xr = x.float().requires_grad_(True)
+    wr = w.float().requires_grad_(True)
+    br = b.clone().requires_grad_(True)
+    yr = torch.nn.functional.conv2d(xr, wr, br, stride=stride, padding=1)
+    yr.backward(gy.to(torch.bfloat16).float())
+    assert _rel(y.float(), yr.detach()) < 1e-2
+    assert _rel(dx, xr.grad) < 1e-2
+    assert _rel(dw, wr.grad) < 1e-2
+    assert _rel(db, br.grad) < 1e-2
+
+
+@pytest.mark.parametrize("N,In,Out", [(1, 5, 7), (37, 200, 130), (300, 2048, 1152), (129, 64, 600)])
+def test_linear_layer_odd_shapes_match_torch(N, In, Out):
+    """Tensor-core linear layer (forward with ReLU into BF16 and FP32 outputs,
+    input, weight and bias gradients) against torch FP32 on the same
+    BF16-rounded operands."""
+    import ctypes
+
+    from leopard_em_gb300._native import lib
+
+    L = lib()
+    g = torch.Generator().manual_seed(N + In + Out)
+    x = torch.randn(N, In, generator=g).to(torch.bfloat16)
+    w = (torch.randn(Out, In, generator=g) / math.sqrt(In)).to(torch.bfloat16)
+    b = torch.randn(Out, generator=g)
+    gy = torch.randn(N, Out, generator=g)
+    xd, wd, bd, gd = x.to(DEV), w.to(DEV), b.to(DEV), gy.to(DEV)
+    ws = _layer_ws(L, L.lgb_nn_linear_workspace_size, N, In, Out)
+    st = torch.zeros(1, dtype=torch.int32, device=DEV)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    ybf = torch.empty(N, Out, dtype=torch.bfloat16, device=DEV)
+    yf = torch.empty(N, Out, device=DEV)
+    assert L.lgb_nn_linear_forward(N, In, Out, 1, xd.data_ptr(), wd.data_ptr(), bd.data_ptr(), ybf.data_ptr(),
+                                   yf.data_ptr(), ws.data_ptr(), ws.numel(), st.data_ptr(), s) == 0
+    dx = torch.empty(N, In, device=DEV)
+    dw = torch.empty(Out, In, device=DEV)
+    db = torch.empty(Out, device=DEV)
+    assert L.lgb_nn_linear_backward(N, In, Out, xd.data_ptr(), wd.data_ptr(), gd.data_ptr(), dx.data_ptr(),
+                                    dw.data_ptr(), db.data_ptr(), ws.data_ptr(), ws.numel(), st.data_ptr(), s) == 0
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0
+    ref = torch.relu(x.float() @ w.float().t() + b)
+    assert _rel(yf, ref) < 1e-4
+    assert torch.equal(ybf.cpu(), yf.cpu().to(torch.bfloat16))
+    gq = gy.to(torch.bfloat16).float()
+    assert _rel(dx, gq @ w.float()) < 1e-2
+    assert _rel(dw, gq.t() @ x.float()) < 1e-2
+    assert _rel(db, gq.sum(0)) < 1e-2
