@@ -476,7 +476,16 @@ class MatchTemplateSearch:
             if self.transpose:
                 res = {k: v.t().contiguous() for k, v in res.items()}
             if to_cpu:
-                res = {k: v.cpu() for k, v in res.items()}
+                # page-locked destinations (torch's caching host allocator reuses
+                # them across calls): the 8 maps go back as asynchronous copies
+                # at full link speed, with one synchronisation
+                host = {}
+                for k, v in res.items():
+                    h = torch.empty(v.shape, dtype=v.dtype, pin_memory=True)
+                    h.copy_(v, non_blocking=True)
+                    host[k] = h
+                torch.cuda.current_stream(dev).synchronize()
+                res = host
         res["total_projections"] = self.total_projections
         res["total_orientations"] = self.problem.n_orientations
         res["total_defocus"] = self.problem.n_defocus

@@ -120,8 +120,9 @@ int launch_rowpass(int W, const void* Y, int H, int y_rows, int Wcp, int n_c, in
     case 2048:
       return rowpass_fused_t<2048, 256, Radices<8, 8, 8, 4>>(Y, H, y_rows, Wcp, n_c, nb, n_orient, o0, o0_dev, mip,
                                                              best, s1, s2, s);
-    case 2880:  // 5760-wide grids (e.g. a 5760 x 4092 micrograph searched transposed); 2 CTAs per SM
-      return rowpass_fused_t<2880, 360, Radices<8, 9, 5, 8>, 2>(Y, H, y_rows, Wcp, n_c, nb, n_orient, o0, o0_dev,
+    case 2880:  // 5760-wide grids (e.g. a 5760 x 4092 micrograph searched transposed): one CTA per SM at
+                // 157 registers without spills (two CTAs at 80 registers spill 324 B and run 9 % slower)
+      return rowpass_fused_t<2880, 360, Radices<8, 9, 5, 8>, 1>(Y, H, y_rows, Wcp, n_c, nb, n_orient, o0, o0_dev,
                                                                 mip, best, s1, s2, s);
     case 1024:
       return rowpass_fused_t<1024, 256, Radices<8, 8, 4, 4>>(Y, H, y_rows, Wcp, n_c, nb, n_orient, o0, o0_dev, mip,
