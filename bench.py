@@ -80,6 +80,10 @@ def _args():
     ap.add_argument("--batched-micrographs", type=int, default=12)
     ap.add_argument("--batched-full-grid", type=int, default=-1,
                     help="only time one batched-workload micrograph (this index) over its full grid")
+    ap.add_argument("--learned-eval", type=int, default=0,
+                    help="only run learned-proposal refinement on this many simulated particles (e.g. 50000)")
+    ap.add_argument("--learned-eval-plain", type=int, default=1024,
+                    help="particles of that set also refined by the plain grid for the SNR comparison")
     ap.add_argument("--batched-orient", type=int, default=48,
                     help="orientations searched per micrograph in the batched-form sample")
     return ap.parse_args()
@@ -541,6 +545,61 @@ def batched_full_grid(args):
             "clocks": clocks.summary()}
 
 
+def learned_eval(args):
+    """Learned-proposal refinement over a large simulated particle set (the
+    refinement configuration's 50,000 crops by default): proposals, small-grid
+    verification and full-grid fallback for every particle, and the plain grid
+    on a seeded subset of them for the SNR comparison.  Not part of the default
+    run (minutes)."""
+    from leopard_em_gb300 import proposal as pr
+    from leopard_em_gb300 import synthetic as sy
+    from leopard_em_gb300.backend.core_refine_template import core_refine_template
+
+    dev = torch.device("cuda", 0)
+    cfg = sy.CONFIG_REFINE
+    n, m = int(args.learned_eval), int(args.learned_eval_plain)
+    t0 = time.perf_counter()
+    parts = []
+    chunk = 4096
+    for a in range(0, n, chunk):  # simulated in chunks (independent seeds), one template
+        kw_a, _ = sy.make_refine_workload(cfg, min(chunk, n - a), device=dev, seed_offset=50_000 + a)
+        parts.append(kw_a)
+    kw = dict(parts[0])
+    for k, v in parts[0].items():
+        if isinstance(v, torch.Tensor) and v.shape[:1] == (min(chunk, n),) and k != "euler_angle_offsets":
+            kw[k] = torch.cat([p[k] for p in parts])
+    del parts
+    t_data = time.perf_counter() - t0
+    net = pr.load_net(os.path.join(ROOT, "leopard_em_gb300", "weights", "proposal_refine288.npz"), dev)
+    small = sy.local_euler_offsets(0.5, 0.125, 0.5, 0.125)
+    small_df = torch.arange(-100.0, 100.0 + 1e-6, 50.0)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    res, info = pr.refine_with_proposals(net, kw, dev, small, small_df, batch_size=cfg.batch)
+    torch.cuda.synchronize(dev)
+    t_learned = time.perf_counter() - t0
+    z = res["refined_z_score"].double()
+    sel = torch.randperm(n, generator=torch.Generator().manual_seed(7))[:m].sort().values
+    sub = {k: (v[sel] if isinstance(v, torch.Tensor) and v.shape[:1] == (n,) else v) for k, v in kw.items()}
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    plain = core_refine_template(**sub, device=dev, batch_size=cfg.batch)
+    torch.cuda.synchronize(dev)
+    t_plain = time.perf_counter() - t0
+    zp, zl = plain["refined_z_score"].double(), z[sel]
+    return {"metric": "learned-proposal refinement over a large simulated particle set",
+            "workload": cfg.name, "particles": n, "data_seconds": t_data,
+            "learned": {"value": n / t_learned, "unit": "particles/s", "seconds": t_learned,
+                        "fallbacks": info["fallback"], "fallback_rate": info["fallback"] / n,
+                        "correlations_per_particle": info["correlations_per_particle"],
+                        "mean_refined_snr": float(z.mean())},
+            "plain_subset": {"particles": m, "value": m / t_plain, "unit": "particles/s",
+                             "mean_refined_snr": float(zp.mean()), "learned_mean_refined_snr": float(zl.mean()),
+                             "learned_at_least_plain": bool(zl.mean() >= zp.mean()),
+                             "particles_below_plain": int((zl < zp - 1e-6).sum())},
+            "timing": "wall clock, host tensors in and out"}
+
+
 def refine_plain_only(args):
     """Plain refinement grid alone (device-timed particles/s), for profiling."""
     from leopard_em_gb300 import synthetic as sy
@@ -752,6 +811,9 @@ def main():
     args = _args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.learned_eval > 0:
+        print(json.dumps(learned_eval(args)), flush=True)
         return
     if args.refine_plain_only:
         print(json.dumps(refine_plain_only(args)), flush=True)
