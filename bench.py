@@ -781,11 +781,16 @@ def run_reference(args):
         return
     from leopard_em_gb300 import synthetic as sy
 
-    cfg = sy.CONFIG_PRODUCTION if args.config == "production" else sy.CONFIG_SMALL
+    cfg = {"production": sy.CONFIG_PRODUCTION, "small": sy.CONFIG_SMALL, "refbench": sy.CONFIG_REFBENCH}[args.config]
     dev = "cuda" if torch.cuda.is_available() else "cpu"
     wl = sy.make_match_workload(cfg, device=dev)
     threads = os.cpu_count() or 1
-    per_step = 1 if args.config == "production" else 8
+    per_step = 1 if args.config in ("production", "refbench") else 8
+    # the orientation batch our arm reports for this workload (the CPU oracle's
+    # correlograms do not depend on it)
+    B = args.batch if args.batch > 0 else cfg.orientation_batch
+    if args.batch < 0 and args.config in ("production", "refbench"):
+        B = 16
     for i in range(args.warmup):
         _cpu_oracle_rate(wl.kwargs, per_step, cfg.orientation_batch, threads, start=i * per_step)
     t0 = time.perf_counter()
@@ -801,7 +806,7 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
         "config": {"workload": cfg.name, "image": list(cfg.image_shape), "template": cfg.template_size,
-                   "defocus_planes": len(cfg.defocus_offsets), "orientation_batch": cfg.orientation_batch},
+                   "defocus_planes": len(cfg.defocus_offsets), "orientation_batch": B},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
