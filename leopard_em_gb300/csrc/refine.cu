@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(NT)
 // leaves pixel pairs m = t + R1*r in thread t.  Same keys and reduction as
 // refine_rowpass_kernel.
 template <int R1, int R2, int ROWS>
-__global__ void __launch_bounds__(ROWS* R1)
+__global__ void __launch_bounds__(ROWS* R1, 3)
     refine_rowpass_pair_kernel(const float2* __restrict__ Y, int y_rows, int Wcp, int n_cpp, int c_per_block,
                                int crop_w, float scale, const float* __restrict__ corr_mean,
                                const float* __restrict__ corr_std, int crop_h,
