@@ -55,7 +55,7 @@ def _args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--orient-per-step", type=int, default=96)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=6)
     ap.add_argument("--e2e-orient", type=int, default=1536,
                     help="orientations per end-to-end call (a slice of the grid, as a caller splitting the search)")
     ap.add_argument("--cpu-sample-orient", type=int, default=4)
@@ -1000,6 +1000,7 @@ def main():
                        "parallelism": f"orientation-sharded x{world}"},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "orientations_per_call": e2e_chunk, "two_run_model": two_run,
+                    "call_ms": [round(1e3 * t, 2) for t in e2e_times],
                     "timing": "wall clock per core_match_template call on pinned host tensors: upload, search, "
                               "finalize, all maps back to the host"},
             "roofline": roofline, "cpu_baseline": cpu, "gpu_torch_baseline": torch_ref,
