@@ -606,6 +606,70 @@ __global__ void __launch_bounds__(ROWS* FftThreads<WH>::value)
   for (int k = WH + 1 + t; k < Wcp; k += NT) out[k] = make_float2(0.f, 0.f);
 }
 
+// pad_rfft for long rows (WH >= 1024, where a CTA holds too few rows for the
+// static form to carry twiddle tables): the CTA fills the FFT and post-twiddle
+// tables once in dynamic shared memory and walks RPC rows of one correlogram,
+// ROWS at a time.  The normalisation constants come precomputed (norm_constants_kernel).
+template <int WH, int ROWS>
+struct PadRows {
+  static constexpr int NT = FftThreads<WH>::value;
+  static constexpr int ZS = IdxPad16::pad(WH) + 2;
+  static constexpr size_t SMEM = sizeof(float2) * ((size_t)ROWS * ZS + FftTable<WH>::SIZE + 1 + WH + 1);
+  static constexpr int MINB = 3 * SMEM <= 227 * 1024 ? 3 : 2;  // CTAs per SM the shared memory allows
+};
+
+template <int WH, int ROWS, int RPC>
+__global__ void __launch_bounds__(ROWS* FftThreads<WH>::value, (PadRows<WH, ROWS>::MINB))
+    pad_rfft_rows_kernel(const float* __restrict__ proj, const double* __restrict__ rowstats, int h, int Wcp,
+                         float2* __restrict__ A) {
+  using PR = PadRows<WH, ROWS>;
+  constexpr int NT = PR::NT, ZS = PR::ZS;
+  extern __shared__ float2 prsm[];
+  float2* z = prsm;                            // [ROWS][ZS]
+  float2* tab = z + ROWS * ZS;                 // FftTable<WH>::SIZE
+  float2* post = tab + FftTable<WH>::SIZE + 1;  // exp(-i pi k / WH), k = 0..WH
+  fill_fft_table<WH>(tab, threadIdx.x, blockDim.x);
+  for (int k = threadIdx.x; k <= WH; k += blockDim.x) {
+    float sn, cs;
+    sincospif((float)k / (float)WH, &sn, &cs);
+    post[k] = make_float2(cs, -sn);
+  }
+  const int c = blockIdx.y;
+  const float2 es = *reinterpret_cast<const float2*>(rowstats + (size_t)c * h * 3);
+  const float e = es.x, s = es.y;
+  const int g = threadIdx.x / NT, t = threadIdx.x - (threadIdx.x / NT) * NT;
+  float2* zg = z + g * ZS;
+  const int nz = (h + 1) / 2;
+  const int y_end = min(h, (int)blockIdx.x * RPC + RPC);
+#pragma unroll 1
+  for (int y0 = blockIdx.x * RPC; y0 < y_end; y0 += ROWS) {
+    const int y = y0 + g;
+    const bool active = y < y_end;
+    if (active) {
+      const float* p = proj + ((size_t)c * h + y) * h;
+      for (int m = t; m < nz; m += NT) {
+        const float a = (p[2 * m] - e) * s;
+        const float b = (2 * m + 1 < h) ? (p[2 * m + 1] - e) * s : 0.f;
+        zg[IdxPad16::f(m)] = make_float2(a, b);
+      }
+    }
+    __syncthreads();  // rows staged; tables filled (first iteration)
+    block_fft_pruned_tab<WH, NT, -1, IdxPad16>(zg, tab, t, nz);
+    if (active) {
+      float2* out = A + ((size_t)c * h + y) * Wcp;
+      for (int k = t; k <= WH; k += NT) {
+        const float2 Zk = zg[IdxPad16::f(k == WH ? 0 : k)];
+        const float2 Zm = cconj(zg[IdxPad16::f(k == 0 ? 0 : WH - k)]);
+        const float2 xe = cscale(cadd(Zk, Zm), 0.5f);
+        const float2 xo = mul_i<-1>(cscale(csub(Zk, Zm), 0.5f));
+        out[k] = cadd(xe, cmul(post[k], xo));
+      }
+      for (int k = WH + 1 + t; k < Wcp; k += NT) out[k] = make_float2(0.f, 0.f);
+    }
+    __syncthreads();  // this pass's rows are read before the next ones are staged
+  }
+}
+
 // Columns per colpass CTA: kColGroup, or 2 where four transforms of length HN
 // would need more than 1024 threads (HN = 5760).
 template <int HN>

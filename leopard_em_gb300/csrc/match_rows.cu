@@ -46,25 +46,39 @@ template <int WH>
 static int pad_rfft_t(const float* proj, const double* rowstats, int h, int norm_h, int norm_w, int Wcp, int n_c,
                       void* A, cudaStream_t s) {
   constexpr int NT = FftThreads<WH>::value;
-  // at least one full warp: the normalisation reduction shuffles across warp 0
-  constexpr int ROWS0 = NT >= 128 ? 2 : (NT >= 32 ? 4 : (NT >= 16 ? 8 : 16));
-  constexpr int ROWS1 = ROWS0 * NT >= 32 ? ROWS0 : (32 + NT - 1) / NT;
-  // static shared memory (ROWS rows of the padded transform) stays under 40 KB
-  constexpr int ROWS = ROWS1 * (IdxPad16::pad(WH) + 2) * 8 <= 40960 ? ROWS1 : 1;
-  static_assert(ROWS * NT >= 32, "pad_rfft CTA must hold a full warp");
-  const int ctas = (h + ROWS - 1) / ROWS;
-  // precompute the constants when many CTAs share a correlogram (each would
-  // otherwise reduce all h rows in FP64); a few CTAs do it themselves
-  const int ready = ctas >= 16;
-  if (ready) {
-    const int st = launch_norm_constants(const_cast<double*>(rowstats), n_c, h, norm_h, norm_w, s);
+  if constexpr (WH >= 1024) {
+    // long rows: tables in dynamic shared memory, 32 rows per CTA, constants precomputed
+    constexpr int ROWS = 2, RPC = 32;
+    using PR = PadRows<WH, ROWS>;
+    int st = launch_norm_constants(const_cast<double*>(rowstats), n_c, h, norm_h, norm_w, s);
     if (st) return st;
+    if (cudaFuncSetAttribute(pad_rfft_rows_kernel<WH, ROWS, RPC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)PR::SMEM) != cudaSuccess)
+      return LGB_ERR_CUDA;
+    pad_rfft_rows_kernel<WH, ROWS, RPC><<<dim3((h + RPC - 1) / RPC, n_c), ROWS * NT, PR::SMEM, s>>>(
+        proj, rowstats, h, Wcp, static_cast<float2*>(A));
+    return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
+  } else {
+    // at least one full warp: the normalisation reduction shuffles across warp 0
+    constexpr int ROWS0 = NT >= 128 ? 2 : (NT >= 32 ? 4 : (NT >= 16 ? 8 : 16));
+    constexpr int ROWS1 = ROWS0 * NT >= 32 ? ROWS0 : (32 + NT - 1) / NT;
+    // static shared memory (ROWS rows of the padded transform) stays under 40 KB
+    constexpr int ROWS = ROWS1 * (IdxPad16::pad(WH) + 2) * 8 <= 40960 ? ROWS1 : 1;
+    static_assert(ROWS * NT >= 32, "pad_rfft CTA must hold a full warp");
+    const int ctas = (h + ROWS - 1) / ROWS;
+    // precompute the constants when many CTAs share a correlogram (each would
+    // otherwise reduce all h rows in FP64); a few CTAs do it themselves
+    const int ready = ctas >= 16;
+    if (ready) {
+      const int st = launch_norm_constants(const_cast<double*>(rowstats), n_c, h, norm_h, norm_w, s);
+      if (st) return st;
+    }
+    dim3 grid(ctas, n_c);
+    // shared twiddle tables where a CTA transforms >= 4 rows
+    pad_rfft_kernel<WH, ROWS, (ROWS >= 4)><<<grid, ROWS * NT, 0, s>>>(proj, rowstats, h, norm_h, norm_w, Wcp,
+                                                                      ready, static_cast<float2*>(A));
+    return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
   }
-  dim3 grid(ctas, n_c);
-  // shared twiddle tables where a CTA transforms >= 4 rows
-  pad_rfft_kernel<WH, ROWS, (ROWS >= 4)><<<grid, ROWS * NT, 0, s>>>(proj, rowstats, h, norm_h, norm_w, Wcp, ready,
-                                                                    static_cast<float2*>(A));
-  return cudaGetLastError() == cudaSuccess ? LGB_OK : LGB_ERR_CUDA;
 }
 
 template <int WH>
