@@ -647,6 +647,40 @@ class RefineTemplateManager(ConfigModel):
         return core_refine_template(**kw, batch_size=orientation_batch_size,
                                     num_cuda_streams=self.computational_config.num_cpus)
 
+    def run_refine_template_learned(self, orientation_batch_size: int = 64, weights_path: Optional[str] = None,
+                                    proposal: Literal["network", "gauss_newton"] = "network",
+                                    small_offsets: Optional[torch.Tensor] = None,
+                                    small_defocus: Optional[torch.Tensor] = None):
+        """Refinement with learned proposals (no reference counterpart; see
+        ``proposal.refine_with_proposals``): the proposal network (the shipped
+        weights unless ``weights_path``) or the Gauss-Newton step proposes each
+        particle's pose and defocus, a small plain grid around the proposal
+        (default +-0.5 deg at 0.125 deg x +-100 A at 50 A) scores it, and every
+        particle whose proposal does not beat its starting pose falls back to
+        this manager's full plain grid.  Crops must be at least 128 x 128 (the
+        network sees the 64 x 64 lowest-frequency band).
+
+        Returns (result, info): ``result`` has the keys of
+        ``run_refine_template``; ``info`` counts the fallbacks."""
+        from . import proposal as pr
+        from .backend.core_match_template import _single_cuda_device
+        from .grids import local_euler_offsets
+
+        box_h, box_w = self.particle_stack.extracted_box_size
+        if box_h < 2 * pr.BAND or box_w < 2 * pr.BAND:
+            raise ValueError(f"learned proposals need crops of at least {2 * pr.BAND} x {2 * pr.BAND}, "
+                             f"got {box_h} x {box_w}; use run_refine_template")
+        kw = self.make_backend_core_function_kwargs()
+        dev = _single_cuda_device(kw.pop("device"))
+        net = None
+        if proposal == "network":
+            path = weights_path or os.path.join(os.path.dirname(__file__), "weights", "proposal_refine288.npz")
+            net = pr.load_net(path, dev)
+        small = small_offsets if small_offsets is not None else local_euler_offsets(0.5, 0.125, 0.5, 0.125)
+        small_df = small_defocus if small_defocus is not None else torch.arange(-100.0, 100.0 + 1e-6, 50.0)
+        return pr.refine_with_proposals(net, kw, dev, small, small_df, batch_size=orientation_batch_size,
+                                        proposal=proposal)
+
     def get_refine_result(self, backend_kwargs: dict, orientation_batch_size: int = 64) -> dict:
         """Refinement results as numpy arrays (refine_template_manager.py:314-353)."""
         res = core_refine_template(**backend_kwargs, batch_size=orientation_batch_size,

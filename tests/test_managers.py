@@ -232,6 +232,9 @@ def test_particle_stack_and_refine_kwargs(tmp_path):
     bad = dict(df_path=csv_path, extracted_box_size=(32, 32), original_template_size=(32, 32))
     with pytest.raises(ValueError):
         m.ParticleStack(**bad)
+    # learned proposals see a 64 x 64 band: 64-pixel crops are refused before any device work
+    with pytest.raises(ValueError, match="at least 128"):
+        mgr.run_refine_template_learned()
 
 
 # ---------------------------------------------------------------------------
@@ -283,3 +286,24 @@ def test_refine_manager_from_yaml_recovers_planted_poses(tmp_path):
     err = angular_error_deg(euler_zyz_to_rotmat(eul.double()), euler_zyz_to_rotmat(planted))
     assert float(err.max()) <= 2.0 * 2.0**0.5 + 1e-3, (eul, planted, err)
     assert np.allclose(np.asarray(res["refined_pos_y"]).reshape(-1), 0.0, atol=1.0)
+
+
+@pytest.mark.gpu
+def test_refine_manager_learned_proposals_run_through_the_manager(tmp_path):
+    """run_refine_template_learned on 128-pixel crops: the same result keys and
+    shapes as the plain grid, every particle either accepted from its proposal
+    or refined by the manager's full grid, and the planted particles found."""
+    wl, mic, tmpl = _match_files(tmp_path)
+    csv_path = _particle_files(tmp_path, wl, mic, tmpl)
+    path = _substituted("refine_template_config.yaml", tmp_path, TEMPLATE=tmpl, PARTICLES=csv_path)
+    mgr = m.RefineTemplateManager.from_yaml(path)
+    mgr.particle_stack.extracted_box_size = (128, 128)
+    plain = mgr.run_refine_template(orientation_batch_size=16)
+    for which in ("network", "gauss_newton"):
+        res, info = mgr.run_refine_template_learned(orientation_batch_size=16, proposal=which)
+        assert set(res) == set(plain) and info["particles"] == 2 and 0 <= info["fallback"] <= 2
+        for k, v in plain.items():
+            if isinstance(v, torch.Tensor):
+                assert tuple(torch.as_tensor(res[k]).shape) == tuple(v.shape), k
+        z = torch.as_tensor(res["refined_z_score"]).reshape(-1)
+        assert bool((z > 5.0).all()), (which, z)
