@@ -43,7 +43,7 @@ def _ctf_params(ctf_kwargs: dict) -> CtfParams:
 
 def refine_particles_device(particle_stack_dft, template_dft, euler_angles, euler_angle_offsets, defocus_offsets,
                             defocus_u, defocus_v, defocus_angle, pixel_size_offsets, corr_mean, corr_std, ctf_kwargs,
-                            projective_filters, device, batch_size=32, max_correlograms_per_call=2048):
+                            projective_filters, device, batch_size=32, max_correlograms_per_call=8192):
     """Run the local grid for every particle; returns raw per-particle device
     results (best z, its batch's max cc, flat index, batch start, batch length)."""
     dev = _device(device)
@@ -55,6 +55,10 @@ def refine_particles_device(particle_stack_dft, template_dft, euler_angles, eule
     B = int(batch_size)
     if B < 1:
         raise ValueError("batch_size must be >= 1")
+    # an offset batch never needs more slots than there are offsets: with few
+    # offsets (e.g. one starting pose) more particles then share each call
+    # (one batch either way, so the tie order is unchanged)
+    B = max(1, min(B, K))
     crop_h, crop_w = H - d + 1, W - d + 1
     if tuple(corr_mean.shape) != (N, crop_h, crop_w) or tuple(corr_std.shape) != (N, crop_h, crop_w):
         raise ValueError(f"corr_mean / corr_std must be (N, {crop_h}, {crop_w})")

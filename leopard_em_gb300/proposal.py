@@ -354,6 +354,13 @@ def refine_with_proposals(net: ProposalNet | None, kwargs: dict, device, small_o
     if proposal not in ("network", "gauss_newton"):
         raise ValueError(f"proposal must be 'network' or 'gauss_newton', got {proposal!r}")
     dev = torch.device(device)
+    # the template and the per-particle images, filters and statistics maps go
+    # to the device once: the input builder and the refinement calls below
+    # would each upload them again
+    kwargs = dict(kwargs)
+    for k in ("particle_stack_dft", "template_dft", "corr_mean", "corr_std", "projective_filters"):
+        if isinstance(kwargs.get(k), torch.Tensor):
+            kwargs[k] = kwargs[k].to(dev)
     ctf = _ctf_params(kwargs["ctf_kwargs"])
     e0 = kwargs["euler_angles"].to(torch.float64)
     r0 = rot.euler_zyz_to_rotmat(e0)
@@ -382,7 +389,7 @@ def refine_with_proposals(net: ProposalNet | None, kwargs: dict, device, small_o
     n_fb = int(fb.sum())
     if n_fb:
         sel = torch.nonzero(fb).flatten()
-        sub = {k: (v[sel] if isinstance(v, torch.Tensor) and v.shape[:1] == fb.shape else v)
+        sub = {k: (v[sel.to(v.device)] if isinstance(v, torch.Tensor) and v.shape[:1] == fb.shape else v)
                for k, v in kwargs.items()}
         res_f = core_refine_template(**sub, device=dev, batch_size=batch_size)
         for k in res:
