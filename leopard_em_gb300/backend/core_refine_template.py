@@ -43,7 +43,7 @@ def _ctf_params(ctf_kwargs: dict) -> CtfParams:
 
 def refine_particles_device(particle_stack_dft, template_dft, euler_angles, euler_angle_offsets, defocus_offsets,
                             defocus_u, defocus_v, defocus_angle, pixel_size_offsets, corr_mean, corr_std, ctf_kwargs,
-                            projective_filters, device, batch_size=32, max_correlograms_per_call=8192):
+                            projective_filters, device, batch_size=32, max_correlograms_per_call=16384):
     """Run the local grid for every particle; returns raw per-particle device
     results (best z, its batch's max cc, flat index, batch start, batch length)."""
     dev = _device(device)
