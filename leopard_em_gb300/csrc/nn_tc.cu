@@ -14,7 +14,8 @@
 // transposed form (outputs as rows) so the epilogue's stores are coalesced.  The
 // output gradient g (FP32) enters the tensor cores rounded to BF16, like the
 // activations; accumulation stays FP32.  The bias gradient is one more column
-// of the weight-gradient GEMM (a row of ones in its B operand).  No reference counterpart (Leopard-EM has no learned component).
+// of the weight-gradient GEMM (a row of ones in its operand).  No reference
+// counterpart (Leopard-EM has no learned component).
 #include <cuda_bf16.h>
 
 #include "tc_gemm.cuh"
@@ -25,8 +26,7 @@ using bf16t = __nv_bfloat16;
 
 struct ConvShape {
   int N, Cin, H, W, Cout, s, Ho, Wo;
-  int P, Q, K, Kt;  // output pixels, input pixels, Cin*9, Cout*9
-  __host__ __device__ int ho_of(int y) const { return (y - 1) / s + 1; }
+  int P, Q, K, Kt;  // output pixels, input pixels, Cin*9, Cout*9 (P, Q < 2^23: checked by the entry points)
 };
 
 static ConvShape conv_shape(int N, int Cin, int H, int W, int Cout, int s) {
