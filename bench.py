@@ -80,6 +80,8 @@ def _args():
     ap.add_argument("--batched-micrographs", type=int, default=12)
     ap.add_argument("--batched-full-grid", type=int, default=-1,
                     help="only time one batched-workload micrograph (this index) over its full grid")
+    ap.add_argument("--precision-stage-4096", action="store_true",
+                    help="only time one radix-64 DFT-GEMM stage at the 4096^2 production shape")
     ap.add_argument("--learned-eval", type=int, default=0,
                     help="only run learned-proposal refinement on this many simulated particles (e.g. 50000)")
     ap.add_argument("--learned-eval-plain", type=int, default=1024,
@@ -600,6 +602,52 @@ def learned_eval(args):
             "timing": "wall clock, host tensors in and out"}
 
 
+def precision_stage_4096(args):
+    """One radix-64 DFT-GEMM stage of a factored inverse column transform at
+    the production shape (48 correlograms x 2,049 columns x 64 = 6.29 M rows,
+    K = N = 128 real values = 64 complex points in and out) on the tcgen05
+    GEMM, with one and three BF16 terms: the measured floor of a 4096^2
+    precision form.  Not part of the default run."""
+    import ctypes
+
+    from leopard_em_gb300 import precision as pc
+    from leopard_em_gb300._native import check, lib
+
+    dev = torch.device("cuda", 0)
+    M, K, N = 48 * 2049 * 64, 128, 128
+    g = torch.Generator(device=dev).manual_seed(0)
+    a = torch.randn(M, K, device=dev, generator=g)
+    b = torch.randn(N, K, device=dev, generator=g)
+    a_hi, a_lo = pc.blocked_split(a, 128)
+    b_hi, b_lo = pc.blocked_split(b, 128)
+    del a
+    d = torch.empty((M, N), dtype=torch.float32, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    s = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    out = {"metric": "one radix-64 DFT-GEMM stage at the 4096^2 production shape", "M": M, "N": N, "K": K}
+    for terms in (3, 1):
+        def run():
+            check(lib().lgb_tc_gemm(M // 128, 1, K // 64, 128, 0, terms, a_hi.data_ptr(), a_lo.data_ptr(),
+                                    b_hi.data_ptr(), b_lo.data_ptr(), d.data_ptr(), N, M, N, err.data_ptr(), s),
+                  "lgb_tc_gemm")
+
+        for _ in range(2):
+            run()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record()
+        for _ in range(5):
+            run()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / 5
+        out[f"bf16x{terms}"] = {"ms": ms, "tflops": 2 * M * N * K * terms / (ms / 1e3) / 1e12,
+                                "operand_gb": M * K * 2 * (2 if terms == 3 else 1) / 1e9, "output_gb": M * N * 4 / 1e9}
+    if int(err.item()):
+        raise RuntimeError("lgb_tc_gemm: device status %d" % int(err.item()))
+    return out
+
+
 def refine_plain_only(args):
     """Plain refinement grid alone (device-timed particles/s), for profiling."""
     from leopard_em_gb300 import synthetic as sy
@@ -816,6 +864,9 @@ def main():
     args = _args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.precision_stage_4096:
+        print(json.dumps(precision_stage_4096(args)), flush=True)
         return
     if args.learned_eval > 0:
         print(json.dumps(learned_eval(args)), flush=True)
