@@ -832,6 +832,7 @@ def run_reference(args):
     cfg = {"production": sy.CONFIG_PRODUCTION, "small": sy.CONFIG_SMALL, "refbench": sy.CONFIG_REFBENCH}[args.config]
     dev = "cuda" if torch.cuda.is_available() else "cpu"
     wl = sy.make_match_workload(cfg, device=dev)
+    cpu_kw = {k: (v.cpu() if isinstance(v, torch.Tensor) else v) for k, v in wl.kwargs.items()}  # host copies, once
     threads = os.cpu_count() or 1
     per_step = 1 if args.config in ("production", "refbench") else 8
     # the orientation batch our arm reports for this workload (the CPU oracle's
@@ -840,10 +841,10 @@ def run_reference(args):
     if args.batch < 0 and args.config in ("production", "refbench"):
         B = 16
     for i in range(args.warmup):
-        _cpu_oracle_rate(wl.kwargs, per_step, cfg.orientation_batch, threads, start=i * per_step)
+        _cpu_oracle_rate(cpu_kw, per_step, cfg.orientation_batch, threads, start=i * per_step)
     t0 = time.perf_counter()
     for i in range(args.steps):
-        _cpu_oracle_rate(wl.kwargs, per_step, cfg.orientation_batch, threads, start=(args.warmup + i) * per_step)
+        _cpu_oracle_rate(cpu_kw, per_step, cfg.orientation_batch, threads, start=(args.warmup + i) * per_step)
     dt = time.perf_counter() - t0
     value = args.steps * per_step / dt
     sample = (f"{per_step} orientation(s) x {len(cfg.defocus_offsets)} defocus per step of the {cfg.name} "
