@@ -5,14 +5,15 @@ Workload (production configuration): 4096 x 4096 micrograph (N(0,1) noise +
 300 planted projections at SNR 0.1), 384^3 Gaussian-blob template at
 1.06 A/px, 3 defocus planes (-200/0/+200 A around 10000 A), orientation grid
 2.5 deg out-of-plane / 1.5 deg in-plane (~1.58 M orientations), orientation
-batch 16 (the autotuner's choice for a 4096^2 grid).  All inputs are synthetic
+batch 32 (the fastest measured for a 4096^2 grid: 4,472 against 4,428 at 24
+and 4,351 at 16 orientations/s).  All inputs are synthetic
 and seeded.
 
 One "step" = one chunk of ``--orient-per-step`` consecutive orientations of
-the grid (default 96 = 6 batches of 16 = 288 cross-correlograms), folded into
+the grid (default 96 = 3 batches of 32 = 288 cross-correlograms), folded into
 the running statistics maps, exactly as one slice of a full search.
 ``value``      orientations/s with inputs resident in HBM (device-timed, CUDA
-               events on the launching stream); every batch streams a 3.2 GB
+               events on the launching stream); every batch streams a 6.4 GB
                correlogram intermediate, far larger than the 129 MB L2.
 ``e2e``        the same metric through the public drop-in
                ``core_match_template`` called with pinned host tensors: every
@@ -63,8 +64,8 @@ def _args():
     ap.add_argument("--config", choices=["production", "small", "refbench"], default="production",
                     help="refbench: the reference's published benchmark shape (4096^2, 512^3, 11 defocus)")
     ap.add_argument("--batch", type=int, default=-1,
-                    help="orientation batch (0: the configuration's; -1: 16 for the production and reference-"
-                         "benchmark shapes, which the autotuner picks for a 4096^2 grid, else the configuration's)")
+                    help="orientation batch (0: the configuration's; -1: 32 for the production and reference-"
+                         "benchmark shapes, the fastest measured for a 4096^2 grid, else the configuration's)")
     ap.add_argument("--refine-particles", type=int, default=128)
     ap.add_argument("--no-refine", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
@@ -839,7 +840,7 @@ def run_reference(args):
     # correlograms do not depend on it)
     B = args.batch if args.batch > 0 else cfg.orientation_batch
     if args.batch < 0 and args.config in ("production", "refbench"):
-        B = 16
+        B = 32
     for i in range(args.warmup):
         _cpu_oracle_rate(cpu_kw, per_step, cfg.orientation_batch, threads, start=i * per_step)
     t0 = time.perf_counter()
@@ -893,7 +894,7 @@ def main():
     N = kw["euler_angles"].shape[0]
     B = args.batch if args.batch > 0 else cfg.orientation_batch
     if args.batch < 0 and args.config in ("production", "refbench"):
-        B = 16
+        B = 32
     chunk = max(B, (args.orient_per_step // B) * B)
     search = MatchTemplateSearch(**kw, device=dev, orientation_batch_size=B)
     stream = torch.cuda.current_stream(dev)
@@ -950,9 +951,10 @@ def main():
     ach = alg_bytes.get(top, 0.0) / (per_launch_ms / 1e3) / 1e9 if top in alg_bytes else None
     # DRAM bytes (read + write) of one launch, from ncu captures of this
     # workload (dram__bytes_read.sum + dram__bytes_write.sum; one launch each,
-    # --set full) at orientation batch 8 and 16
+    # --set full) at orientation batch 8, 16 and 32
     measured_traffic = {("production", 8, "colpass"): 1.875e9, ("production", 8, "rowpass"): 2.390e9,
-                        ("production", 16, "colpass"): 3.657e9, ("production", 16, "rowpass"): 4.042e9}
+                        ("production", 16, "colpass"): 3.657e9, ("production", 16, "rowpass"): 4.042e9,
+                        ("production", 32, "colpass"): 7.357e9, ("production", 32, "rowpass"): 7.282e9}
     roofline = {
         "bound": "hbm", "kernel": top, "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
         "frac": (ach / peaks["hbm_gbs"]) if ach else None,

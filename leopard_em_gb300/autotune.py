@@ -32,7 +32,7 @@ import torch
 from ._native import lib
 
 CACHE_ENV = "LEOPARD_EM_GB300_TUNE_CACHE"
-DEFAULT_BATCHES = (2, 4, 8, 12, 16)
+DEFAULT_BATCHES = (2, 4, 8, 12, 16, 24, 32)
 DEFAULT_WAVES = (2, 4, 8)
 TRANSPOSE_GAIN = 0.9  # a transposed grid must time at most this fraction of the best direct one
 _lock = threading.Lock()
@@ -111,7 +111,7 @@ def _time_candidate(make_search, cand, n_probe: int, repeats: int) -> float:
 
 
 def tune_search(image_dft, template_dft, ctf_filters, whitening_filter_template, defocus_values, pixel_values,
-                euler_angles, device, batches=DEFAULT_BATCHES, waves=DEFAULT_WAVES, n_probe: int = 48,
+                euler_angles, device, batches=DEFAULT_BATCHES, waves=DEFAULT_WAVES, n_probe: int = 96,
                 repeats: int = 2, memory_fraction: float = 0.5, use_cache: bool = True,
                 tune_grid: bool = True) -> SearchTuning:
     """Pick the grid, orientation batch and column split for this search shape.
