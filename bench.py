@@ -5,8 +5,9 @@ Workload (production configuration): 4096 x 4096 micrograph (N(0,1) noise +
 300 planted projections at SNR 0.1), 384^3 Gaussian-blob template at
 1.06 A/px, 3 defocus planes (-200/0/+200 A around 10000 A), orientation grid
 2.5 deg out-of-plane / 1.5 deg in-plane (~1.58 M orientations), orientation
-batch 32 (the fastest measured for a 4096^2 grid: 4,472 against 4,428 at 24
-and 4,351 at 16 orientations/s).  All inputs are synthetic
+batch 32 (the autotuner's choice for a 4096^2 grid, and the fastest measured:
+4,472 against 4,428 at 24 and 4,351 at 16 orientations/s).  All inputs are
+synthetic
 and seeded.
 
 One "step" = one chunk of ``--orient-per-step`` consecutive orientations of
