@@ -7,8 +7,7 @@ Workload (production configuration): 4096 x 4096 micrograph (N(0,1) noise +
 2.5 deg out-of-plane / 1.5 deg in-plane (~1.58 M orientations), orientation
 batch 32 (the autotuner's choice for a 4096^2 grid, and the fastest measured:
 4,472 against 4,428 at 24 and 4,351 at 16 orientations/s).  All inputs are
-synthetic
-and seeded.
+synthetic and seeded.
 
 One "step" = one chunk of ``--orient-per-step`` consecutive orientations of
 the grid (default 96 = 3 batches of 32 = 288 cross-correlograms), folded into
