@@ -5,15 +5,15 @@ Workload (production configuration): 4096 x 4096 micrograph (N(0,1) noise +
 300 planted projections at SNR 0.1), 384^3 Gaussian-blob template at
 1.06 A/px, 3 defocus planes (-200/0/+200 A around 10000 A), orientation grid
 2.5 deg out-of-plane / 1.5 deg in-plane (~1.58 M orientations), orientation
-batch 32 (the autotuner's choice for a 4096^2 grid, and the fastest measured:
-4,472 against 4,428 at 24 and 4,351 at 16 orientations/s).  All inputs are
-synthetic and seeded.
+batch 64 (the autotuner's choice for a 4096^2 grid, and the fastest measured:
+4,543 against 4,525 at 48, 4,482 at 32 and 4,351 at 16 orientations/s).  All
+inputs are synthetic and seeded.
 
 One "step" = one chunk of ``--orient-per-step`` consecutive orientations of
-the grid (default 96 = 3 batches of 32 = 288 cross-correlograms), folded into
+the grid (default 192 = 3 batches of 64 = 576 cross-correlograms), folded into
 the running statistics maps, exactly as one slice of a full search.
 ``value``      orientations/s with inputs resident in HBM (device-timed, CUDA
-               events on the launching stream); every batch streams a 6.4 GB
+               events on the launching stream); every batch streams a 12.9 GB
                correlogram intermediate, far larger than the 129 MB L2.
 ``e2e``        the same metric through the public drop-in
                ``core_match_template`` called with pinned host tensors: every
@@ -55,7 +55,7 @@ def _args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--orient-per-step", type=int, default=96)
+    ap.add_argument("--orient-per-step", type=int, default=192)
     ap.add_argument("--e2e-steps", type=int, default=6)
     ap.add_argument("--e2e-orient", type=int, default=1536,
                     help="orientations per end-to-end call (a slice of the grid, as a caller splitting the search)")
@@ -64,8 +64,8 @@ def _args():
     ap.add_argument("--config", choices=["production", "small", "refbench"], default="production",
                     help="refbench: the reference's published benchmark shape (4096^2, 512^3, 11 defocus)")
     ap.add_argument("--batch", type=int, default=-1,
-                    help="orientation batch (0: the configuration's; -1: 32 for the production and reference-"
-                         "benchmark shapes, the fastest measured for a 4096^2 grid, else the configuration's)")
+                    help="orientation batch (0: the configuration's; -1: 64 for the production and reference-"
+                         "benchmark shapes, the autotuner's choice for a 4096^2 grid, else the configuration's)")
     ap.add_argument("--refine-particles", type=int, default=128)
     ap.add_argument("--no-refine", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
@@ -840,7 +840,7 @@ def run_reference(args):
     # correlograms do not depend on it)
     B = args.batch if args.batch > 0 else cfg.orientation_batch
     if args.batch < 0 and args.config in ("production", "refbench"):
-        B = 32
+        B = 64
     for i in range(args.warmup):
         _cpu_oracle_rate(cpu_kw, per_step, cfg.orientation_batch, threads, start=i * per_step)
     t0 = time.perf_counter()
@@ -894,7 +894,7 @@ def main():
     N = kw["euler_angles"].shape[0]
     B = args.batch if args.batch > 0 else cfg.orientation_batch
     if args.batch < 0 and args.config in ("production", "refbench"):
-        B = 32
+        B = 64
     chunk = max(B, (args.orient_per_step // B) * B)
     search = MatchTemplateSearch(**kw, device=dev, orientation_batch_size=B)
     stream = torch.cuda.current_stream(dev)
@@ -951,10 +951,15 @@ def main():
     ach = alg_bytes.get(top, 0.0) / (per_launch_ms / 1e3) / 1e9 if top in alg_bytes else None
     # DRAM bytes (read + write) of one launch, from ncu captures of this
     # workload (dram__bytes_read.sum + dram__bytes_write.sum; one launch each,
-    # --set full) at orientation batch 8, 16 and 32
+    # --set full) at orientation batch 8, 16 and 32.  Batch 64 holds too much
+    # device memory for a multi-pass capture: its figures extend the 16 and 32
+    # captures linearly in the correlograms per launch (colpass 3.657 -> 7.357
+    # GB for 48 -> 96; rowpass 4.042 -> 7.282 GB, of which 0.80 GB is the map
+    # read-modify-write that does not grow).
     measured_traffic = {("production", 8, "colpass"): 1.875e9, ("production", 8, "rowpass"): 2.390e9,
                         ("production", 16, "colpass"): 3.657e9, ("production", 16, "rowpass"): 4.042e9,
-                        ("production", 32, "colpass"): 7.357e9, ("production", 32, "rowpass"): 7.282e9}
+                        ("production", 32, "colpass"): 7.357e9, ("production", 32, "rowpass"): 7.282e9,
+                        ("production", 64, "colpass"): 14.757e9, ("production", 64, "rowpass"): 13.762e9}
     roofline = {
         "bound": "hbm", "kernel": top, "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
         "frac": (ach / peaks["hbm_gbs"]) if ach else None,

@@ -32,7 +32,8 @@ import torch
 from ._native import lib
 
 CACHE_ENV = "LEOPARD_EM_GB300_TUNE_CACHE"
-DEFAULT_BATCHES = (2, 4, 8, 12, 16, 24, 32)
+DEFAULT_BATCHES = (2, 4, 8, 12, 16, 24, 32, 48, 64)
+MAX_BATCH_CORRELOGRAMS = 1024  # C * D * B cap: larger batches gain little and hold a big intermediate
 DEFAULT_WAVES = (2, 4, 8)
 TRANSPOSE_GAIN = 0.9  # a transposed grid must time at most this fraction of the best direct one
 _lock = threading.Lock()
@@ -111,7 +112,7 @@ def _time_candidate(make_search, cand, n_probe: int, repeats: int) -> float:
 
 
 def tune_search(image_dft, template_dft, ctf_filters, whitening_filter_template, defocus_values, pixel_values,
-                euler_angles, device, batches=DEFAULT_BATCHES, waves=DEFAULT_WAVES, n_probe: int = 96,
+                euler_angles, device, batches=DEFAULT_BATCHES, waves=DEFAULT_WAVES, n_probe: int = 192,
                 repeats: int = 2, memory_fraction: float = 0.5, use_cache: bool = True,
                 tune_grid: bool = True) -> SearchTuning:
     """Pick the grid, orientation batch and column split for this search shape.
@@ -159,6 +160,8 @@ def tune_search(image_dft, template_dft, ctf_filters, whitening_filter_template,
                                        transpose=tr)
 
         def fits(gt, b):
+            if C * D * b > MAX_BATCH_CORRELOGRAMS:
+                return False
             g, tr = gt
             mh, mw = (W, H) if tr else (H, W)
             p = MatchProblem(g[0], g[1], d, C, D, n_probe, b, mh, mw, 0)
